@@ -1,0 +1,256 @@
+/*
+ * atmo.h -- C ABI of the GB300-native atmosphere LUT precomputation.
+ *
+ * Drop-in boundary for the precomputation path of
+ * ebruneton/precomputed_atmospheric_scattering:
+ *
+ *   reference (C++ / OpenGL)                          this ABI
+ *   -----------------------------------------------  ------------------------------
+ *   DensityProfileLayer        atmosphere/model.h:165-178   atmo_density_layer
+ *   Model::Model(19 params)    atmosphere/model.h:182-281   atmo_model_create
+ *   Model::~Model              atmosphere/model.cc:801-811  atmo_model_destroy
+ *   Model::Init(orders)        atmosphere/model.h:285       atmo_model_init
+ *   Model::shader()            atmosphere/model.h:287       atmo_model_shader_source
+ *   Model::SetProgramUniforms  atmosphere/model.h:289-294   atmo_model_get_lut (device
+ *                                                          buffers; GL binding is
+ *                                                          unavailable on this machine)
+ *   Model::ConvertSpectrumToLinearSrgb  model.h:301-304    atmo_convert_spectrum_to_linear_srgb
+ *   kLambdaR/G/B               atmosphere/model.h:306-308   ATMO_LAMBDA_R/G/B
+ *   texture sizes              atmosphere/constants.h:47-61 atmo_lut_shape
+ *   glGetTexImage read-back    atmosphere/demo/webgl/precompute.cc:63-72
+ *                                                          atmo_model_read_lut
+ *
+ * All entry points return an atmo_status.  Plain C types only: device
+ * pointers are exported as integers/void*, streams as opaque pointers that
+ * are CUDA cudaStream_t values (NULL = the legacy default stream).
+ *
+ * Threading: one model / batch / server object per host thread, or an
+ * external lock; work is ordered on the stream given to each call.
+ */
+#ifndef ATMO_ATMO_H_
+#define ATMO_ATMO_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATMO_ABI_VERSION 1
+
+#define ATMO_LAMBDA_R 680.0
+#define ATMO_LAMBDA_G 550.0
+#define ATMO_LAMBDA_B 440.0
+
+typedef struct CUstream_st* atmo_stream;
+
+typedef enum {
+  ATMO_OK = 0,
+  ATMO_INVALID_ARG = 1,   /* NULL pointer, bad size, NaN or inconsistent parameter */
+  ATMO_OOM = 2,           /* device or host allocation failed */
+  ATMO_CUDA_ERROR = 3,    /* a CUDA runtime call failed; see atmo_last_error() */
+  ATMO_TIMEOUT = 4,       /* a bounded wait ran out */
+  ATMO_BUDGET = 5,        /* the request does not fit the device-memory budget */
+  ATMO_UNAVAILABLE = 6,   /* feature not available here (e.g. OpenGL interop) */
+  ATMO_NOT_READY = 7      /* LUTs requested before Init */
+} atmo_status;
+
+/* atmosphere/model.h:165-178: density = exp_term*exp(exp_scale*h)
+   + linear_term*h + constant_term, clamped to [0,1]; h and width in m,
+   exp_scale and linear_term in 1/m. */
+typedef struct {
+  double width, exp_term, exp_scale, linear_term, constant_term;
+} atmo_density_layer;
+
+/* The 19 constructor parameters of atmosphere/model.h:182-281.  Spectral
+   arrays have num_wavelengths entries, sampled at `wavelengths` (nm, sorted). */
+typedef struct {
+  const double* wavelengths;
+  unsigned num_wavelengths;
+  const double* solar_irradiance;              /* W/m^2/nm */
+  double sun_angular_radius;                   /* rad */
+  double bottom_radius;                        /* m */
+  double top_radius;                           /* m */
+  const atmo_density_layer* rayleigh_density;  /* 1 or 2 layers, bottom first */
+  unsigned num_rayleigh_layers;
+  const double* rayleigh_scattering;           /* 1/m */
+  const atmo_density_layer* mie_density;
+  unsigned num_mie_layers;
+  const double* mie_scattering;                /* 1/m */
+  const double* mie_extinction;                /* 1/m */
+  double mie_phase_function_g;
+  const atmo_density_layer* absorption_density;
+  unsigned num_absorption_layers;
+  const double* absorption_extinction;         /* 1/m */
+  const double* ground_albedo;
+  double max_sun_zenith_angle;                 /* rad */
+  double length_unit_in_meters;
+  unsigned num_precomputed_wavelengths;        /* <= 3: radiance; > 3: luminance */
+  int combine_scattering_textures;
+  int half_precision;
+} atmo_model_params;
+
+/* LUT sizes (atmosphere/constants.h:47-61) as run-time values.  A NULL shape
+   selects the reference's defaults: 256x64, NU 8 x MU_S 32 x MU 128 x R 32,
+   64x16.  scattering_mu must be even and every size >= 2. */
+typedef struct {
+  int transmittance_width, transmittance_height;
+  int scattering_r, scattering_mu, scattering_mu_s, scattering_nu;
+  int irradiance_width, irradiance_height;
+} atmo_lut_shape;
+
+/* One precomputation group's atmosphere (atmosphere/definitions.glsl:205-255)
+   at 3 wavelengths, already in length units: what the reference bakes into
+   its GLSL header (atmosphere/model.cc:716-744). */
+typedef struct {
+  atmo_density_layer layers[2];
+} atmo_density_profile;
+
+typedef struct {
+  double solar_irradiance[3];
+  double sun_angular_radius;
+  double bottom_radius;
+  double top_radius;
+  atmo_density_profile rayleigh_density;
+  double rayleigh_scattering[3];
+  atmo_density_profile mie_density;
+  double mie_scattering[3];
+  double mie_extinction[3];
+  double mie_phase_function_g;
+  atmo_density_profile absorption_density;
+  double absorption_extinction[3];
+  double ground_albedo[3];
+  double mu_s_min;
+} atmo_atmosphere;
+
+typedef enum {
+  ATMO_LUT_TRANSMITTANCE = 0,   /* 2D W_T x H_T, float32 RGBA */
+  ATMO_LUT_SCATTERING = 1,      /* 3D (NU*MU_S) x MU x R, float32 or float16 RGBA */
+  ATMO_LUT_SINGLE_MIE = 2,      /* same layout; only when not combined */
+  ATMO_LUT_IRRADIANCE = 3       /* 2D W_I x H_I, float32 RGBA */
+} atmo_lut_kind;
+
+typedef enum { ATMO_DTYPE_F32 = 0, ATMO_DTYPE_F16 = 1 } atmo_dtype;
+
+typedef struct {
+  void* device_ptr;        /* RGBA texels, x fastest, then y, then z */
+  int width, height, depth;
+  atmo_dtype dtype;
+  size_t bytes;
+} atmo_lut_view;
+
+/* Kernel implementation used by Init: the plain per-texel kernels (the
+   reference's per-fragment structure) or the restructured fast kernels. */
+typedef enum { ATMO_PATH_FAST = 0, ATMO_PATH_PLAIN = 1 } atmo_path;
+
+typedef struct atmo_model atmo_model;
+typedef struct atmo_batch atmo_batch;
+
+/* ---- library --------------------------------------------------------------- */
+int atmo_abi_version(void);
+/* Message of the last failing call on this host thread (never NULL). */
+const char* atmo_last_error(void);
+/* Waits for the work enqueued on `stream` (cudaStreamSynchronize). */
+atmo_status atmo_synchronize(atmo_stream stream);
+
+/* ---- Model (atmosphere/model.h) ------------------------------------------- */
+/* Validates and converts the parameters like atmosphere/model.cc:613-745 and
+   allocates the final LUTs on the current CUDA device.  shape may be NULL. */
+atmo_status atmo_model_create(const atmo_model_params* params, const atmo_lut_shape* shape,
+                              atmo_model** out);
+atmo_status atmo_model_destroy(atmo_model* model);
+/* Precomputes the LUTs (atmosphere/model.cc:866-975), ordered on `stream`;
+   returns after the work is enqueued.  num_scattering_orders >= 1. */
+atmo_status atmo_model_init(atmo_model* model, unsigned num_scattering_orders,
+                            atmo_stream stream);
+atmo_status atmo_model_set_path(atmo_model* model, atmo_path path);
+/* exact != 0: compute with the parameters as given instead of the 6-decimal
+   values the reference prints into its GLSL header (model.cc:636-666).
+   Takes effect at the next atmo_model_init. */
+atmo_status atmo_model_set_exact_parameters(atmo_model* model, int exact);
+/* Device buffers of the final LUTs (valid until atmo_model_destroy). */
+atmo_status atmo_model_get_lut(const atmo_model* model, atmo_lut_kind kind,
+                               atmo_lut_view* view);
+/* Copies a LUT to host memory (glGetTexImage equivalent): always float32
+   RGBA, `bytes` must equal width*height*depth*16.  Synchronous. */
+atmo_status atmo_model_read_lut(const atmo_model* model, atmo_lut_kind kind, float* host_dst,
+                                size_t bytes);
+/* The 3-wavelength atmosphere the model computes with for `lambdas` (nm),
+   including the std::to_string rounding of atmosphere/model.cc:636-666 unless
+   the model was created with exact parameters. */
+atmo_status atmo_model_atmosphere_at(const atmo_model* model, const double lambdas[3],
+                                     atmo_atmosphere* out);
+/* GLSL source of the reference's shader() for this model (the header of
+   atmosphere/model.cc:691-744 followed by the API shader of :221-281); the
+   reference's functions.glsl text is not bundled, a marker stands in for it.
+   Writes at most `capacity` bytes (NUL-terminated); *needed gets the size. */
+atmo_status atmo_model_shader_source(const atmo_model* model, char* dst, size_t capacity,
+                                     size_t* needed);
+/* SKY_ and SUN_SPECTRAL_RADIANCE_TO_LUMINANCE (atmosphere/model.cc:663-686). */
+atmo_status atmo_model_luminance_factors(const atmo_model* model, double sky[3],
+                                         double sun[3]);
+/* OpenGL texture binding (atmosphere/model.cc:984-1011): the box has no
+   graphics stack; always returns ATMO_UNAVAILABLE. */
+atmo_status atmo_model_set_program_uniforms(const atmo_model* model, unsigned program,
+                                            unsigned transmittance_unit,
+                                            unsigned scattering_unit,
+                                            unsigned irradiance_unit,
+                                            unsigned single_mie_unit);
+
+/* atmosphere/model.cc:1020-1040 (host computation). */
+atmo_status atmo_convert_spectrum_to_linear_srgb(const double* wavelengths,
+                                                 const double* spectrum, unsigned n,
+                                                 double* r, double* g, double* b);
+
+/* ---- one precomputation group over caller-owned device buffers ------------- */
+/* The Model::Precompute step (atmosphere/model.cc:1048-1215) for one
+   3-wavelength atmosphere: writes transmittance, scattering (and single_mie
+   when !combined) and irradiance, all float32 RGBA device buffers in the
+   layouts above.  lum is the row-major luminance_from_radiance matrix
+   (NULL = identity); blend accumulates like the reference's second and later
+   wavelength groups.  Allocates its temporaries with cudaMallocAsync. */
+atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_shape* shape,
+                            unsigned num_scattering_orders, const float lum[9], int blend,
+                            int combined, atmo_path path, float* transmittance,
+                            float* scattering, float* single_mie, float* irradiance,
+                            atmo_stream stream);
+
+/* ---- batched precomputation (many atmospheres, uneven shapes/orders) ------- */
+/* Creates a batch of n independent atmospheres, each with its own shape and
+   scattering-order count; allocates every instance's LUTs and temporaries. */
+atmo_status atmo_batch_create(const atmo_atmosphere* atmospheres, const atmo_lut_shape* shapes,
+                              const unsigned* num_scattering_orders, unsigned n,
+                              int combined, atmo_batch** out);
+atmo_status atmo_batch_destroy(atmo_batch* batch);
+/* Replaces the parameters of instance i (same shape and order count). */
+atmo_status atmo_batch_set_atmosphere(atmo_batch* batch, unsigned i,
+                                      const atmo_atmosphere* atmosphere);
+/* Runs every instance's full precomputation; the pass sequence is captured
+   in a CUDA graph on first use and replayed afterwards. */
+atmo_status atmo_batch_run(atmo_batch* batch, atmo_stream stream);
+atmo_status atmo_batch_get_lut(const atmo_batch* batch, unsigned i, atmo_lut_kind kind,
+                               atmo_lut_view* view);
+atmo_status atmo_batch_read_lut(const atmo_batch* batch, unsigned i, atmo_lut_kind kind,
+                                float* host_dst, size_t bytes);
+/* Number of kernels one atmo_batch_run launches (for launch accounting). */
+atmo_status atmo_batch_kernel_count(const atmo_batch* batch, unsigned* count);
+/* Runs the batch once without a graph and times every kernel with CUDA
+   events on `stream`: ms[i], pass[i] (0 tables, 1 transmittance, 2 direct
+   irradiance, 3 single scattering, 4 scattering density, 5 indirect
+   irradiance, 6 multiple scattering, 7 FP16 conversion) and order[i] for
+   i < *count (at most `capacity` entries).  Synchronous. */
+atmo_status atmo_batch_time_passes(atmo_batch* batch, atmo_stream stream, unsigned capacity,
+                                   float* ms, int* pass, int* order, unsigned* count);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+/* Measures this GPU's FP32 FMA throughput (TFLOP/s, 2 FLOP per FMA) with a
+   short dependent-chain kernel over every SM: the denominator of the
+   precomputation kernels' FP32 roofline.  Synchronous, ~10 ms. */
+atmo_status atmo_measure_fp32_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATMO_ATMO_H_ */

@@ -1,0 +1,449 @@
+"""GB300-native precomputation of Bruneton's atmospheric-scattering LUTs.
+
+Python mirror of the reference's C++ API (ebruneton/precomputed_atmospheric_
+scattering, atmosphere/model.h): ``DensityProfileLayer``, ``Model`` with the
+same 19 constructor parameters, ``Model.Init(num_scattering_orders=4)``,
+``Model.shader()``, ``Model.SetProgramUniforms`` (unavailable: no graphics
+stack), ``Model.ConvertSpectrumToLinearSrgb`` and ``kLambdaR/G/B``.  Every call
+goes through the C ABI of include/atmo/atmo.h in libatmo_gb300.so (CUDA for
+sm_103a); there is no CPU path: when the library is missing this module raises.
+
+The LUTs stay on the GPU; ``Model.transmittance()`` and friends copy them to
+host numpy arrays in the reference's texture layouts (x fastest: transmittance
+(H, W, 4), scattering (R, MU, NU*MU_S, 4), irradiance (H, W, 4)).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libatmo_gb300.so")
+
+kLambdaR = 680.0
+kLambdaG = 550.0
+kLambdaB = 440.0
+
+OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, BUDGET, UNAVAILABLE, NOT_READY = range(8)
+LUT_TRANSMITTANCE, LUT_SCATTERING, LUT_SINGLE_MIE, LUT_IRRADIANCE = range(4)
+PATH_FAST, PATH_PLAIN = 0, 1
+
+
+class AtmoError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("atmo status %d: %s" % (status, message))
+        self.status = status
+
+
+class Unavailable(AtmoError):
+    pass
+
+
+# ---------------------------------------------------------------------------
+# C structs of include/atmo/atmo.h
+# ---------------------------------------------------------------------------
+class _Layer(C.Structure):
+    _fields_ = [("width", C.c_double), ("exp_term", C.c_double), ("exp_scale", C.c_double),
+                ("linear_term", C.c_double), ("constant_term", C.c_double)]
+
+
+class _ModelParams(C.Structure):
+    _fields_ = [
+        ("wavelengths", C.POINTER(C.c_double)), ("num_wavelengths", C.c_uint),
+        ("solar_irradiance", C.POINTER(C.c_double)), ("sun_angular_radius", C.c_double),
+        ("bottom_radius", C.c_double), ("top_radius", C.c_double),
+        ("rayleigh_density", C.POINTER(_Layer)), ("num_rayleigh_layers", C.c_uint),
+        ("rayleigh_scattering", C.POINTER(C.c_double)),
+        ("mie_density", C.POINTER(_Layer)), ("num_mie_layers", C.c_uint),
+        ("mie_scattering", C.POINTER(C.c_double)), ("mie_extinction", C.POINTER(C.c_double)),
+        ("mie_phase_function_g", C.c_double),
+        ("absorption_density", C.POINTER(_Layer)), ("num_absorption_layers", C.c_uint),
+        ("absorption_extinction", C.POINTER(C.c_double)),
+        ("ground_albedo", C.POINTER(C.c_double)),
+        ("max_sun_zenith_angle", C.c_double), ("length_unit_in_meters", C.c_double),
+        ("num_precomputed_wavelengths", C.c_uint),
+        ("combine_scattering_textures", C.c_int), ("half_precision", C.c_int),
+    ]
+
+
+class LutShape(C.Structure):
+    """atmosphere/constants.h:47-61 as run-time sizes."""
+    _fields_ = [("transmittance_width", C.c_int), ("transmittance_height", C.c_int),
+                ("scattering_r", C.c_int), ("scattering_mu", C.c_int),
+                ("scattering_mu_s", C.c_int), ("scattering_nu", C.c_int),
+                ("irradiance_width", C.c_int), ("irradiance_height", C.c_int)]
+
+    @classmethod
+    def of(cls, shape):
+        if shape is None:
+            return None
+        if isinstance(shape, cls):
+            return shape
+        return cls(*[int(v) for v in shape])
+
+    def as_tuple(self):
+        return tuple(getattr(self, f) for f, _ in self._fields_)
+
+
+DEFAULT_SHAPE = (256, 64, 32, 128, 32, 8, 64, 16)
+
+
+class _Profile(C.Structure):
+    _fields_ = [("layers", _Layer * 2)]
+
+
+_D3 = C.c_double * 3
+
+
+class Atmosphere(C.Structure):
+    """One wavelength group's AtmosphereParameters (atmosphere/definitions.glsl:
+    205-255) at 3 wavelengths, in length units."""
+    _fields_ = [
+        ("solar_irradiance", _D3), ("sun_angular_radius", C.c_double),
+        ("bottom_radius", C.c_double), ("top_radius", C.c_double),
+        ("rayleigh_density", _Profile), ("rayleigh_scattering", _D3),
+        ("mie_density", _Profile), ("mie_scattering", _D3), ("mie_extinction", _D3),
+        ("mie_phase_function_g", C.c_double),
+        ("absorption_density", _Profile), ("absorption_extinction", _D3),
+        ("ground_albedo", _D3), ("mu_s_min", C.c_double),
+    ]
+
+    @classmethod
+    def from_buffer_of(cls, other):
+        """Copies any ctypes struct with this layout (e.g. the oracle's)."""
+        a = cls()
+        C.memmove(C.byref(a), C.byref(other), C.sizeof(cls))
+        return a
+
+
+class LutView(C.Structure):
+    _fields_ = [("device_ptr", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
+                ("depth", C.c_int), ("dtype", C.c_int), ("bytes", C.c_size_t)]
+
+
+# ---------------------------------------------------------------------------
+# Library loading
+# ---------------------------------------------------------------------------
+_lib = None
+
+
+def build(verbose=False, force=False):
+    """Compiles libatmo_gb300.so for sm_103a (nvcc)."""
+    from . import nvcc_build as _b
+    return _b.build(verbose=verbose, force=force)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                "libatmo_gb300.so is not built: run precomputed_atmospheric_scattering_gb300."
+                "build() (there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        P, st = C.POINTER, C.c_int
+        vp = C.c_void_p
+        L.atmo_abi_version.restype = C.c_int
+        L.atmo_last_error.restype = C.c_char_p
+        sigs = {
+            "atmo_synchronize": [vp],
+            "atmo_model_create": [P(_ModelParams), P(LutShape), P(vp)],
+            "atmo_model_destroy": [vp],
+            "atmo_model_init": [vp, C.c_uint, vp],
+            "atmo_model_set_path": [vp, C.c_int],
+            "atmo_model_set_exact_parameters": [vp, C.c_int],
+            "atmo_model_get_lut": [vp, C.c_int, P(LutView)],
+            "atmo_model_read_lut": [vp, C.c_int, P(C.c_float), C.c_size_t],
+            "atmo_model_atmosphere_at": [vp, P(C.c_double), P(Atmosphere)],
+            "atmo_model_shader_source": [vp, C.c_char_p, C.c_size_t, P(C.c_size_t)],
+            "atmo_model_luminance_factors": [vp, P(C.c_double), P(C.c_double)],
+            "atmo_model_set_program_uniforms": [vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                                                C.c_uint],
+            "atmo_convert_spectrum_to_linear_srgb": [P(C.c_double), P(C.c_double), C.c_uint,
+                                                     P(C.c_double), P(C.c_double),
+                                                     P(C.c_double)],
+            "atmo_precompute": [P(Atmosphere), P(LutShape), C.c_uint, P(C.c_float), C.c_int,
+                                C.c_int, C.c_int, vp, vp, vp, vp, vp],
+            "atmo_batch_create": [P(Atmosphere), P(LutShape), P(C.c_uint), C.c_uint, C.c_int,
+                                  P(vp)],
+            "atmo_batch_destroy": [vp],
+            "atmo_batch_set_atmosphere": [vp, C.c_uint, P(Atmosphere)],
+            "atmo_batch_run": [vp, vp],
+            "atmo_batch_get_lut": [vp, C.c_uint, C.c_int, P(LutView)],
+            "atmo_batch_read_lut": [vp, C.c_uint, C.c_int, P(C.c_float), C.c_size_t],
+            "atmo_batch_kernel_count": [vp, P(C.c_uint)],
+            "atmo_measure_fp32_peak": [P(C.c_double)],
+            "atmo_batch_time_passes": [vp, vp, C.c_uint, P(C.c_float), P(C.c_int), P(C.c_int),
+                                       P(C.c_uint)],
+        }
+        for name, args in sigs.items():
+            f = getattr(L, name)
+            f.restype = st
+            f.argtypes = args
+        if L.atmo_abi_version() != 1:
+            raise ImportError("libatmo_gb300.so ABI version mismatch")
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != OK:
+        msg = lib().atmo_last_error().decode()
+        if status == UNAVAILABLE:
+            raise Unavailable(status, msg)
+        raise AtmoError(status, msg)
+
+
+def _dptr(a):
+    return np.ascontiguousarray(a, np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+# ---------------------------------------------------------------------------
+# Reference API
+# ---------------------------------------------------------------------------
+class DensityProfileLayer:
+    """atmosphere/model.h:165-178 (width in m, exp_scale/linear_term in 1/m)."""
+
+    def __init__(self, width=0.0, exp_term=0.0, exp_scale=0.0, linear_term=0.0,
+                 constant_term=0.0):
+        self.width = width
+        self.exp_term = exp_term
+        self.exp_scale = exp_scale
+        self.linear_term = linear_term
+        self.constant_term = constant_term
+
+    def _c(self):
+        return _Layer(self.width, self.exp_term, self.exp_scale, self.linear_term,
+                      self.constant_term)
+
+
+def _layers(ls):
+    arr = (_Layer * max(1, len(ls)))(*[l._c() for l in ls])
+    return arr, len(ls)
+
+
+class Model:
+    """atmosphere/model.h:180-337 over CUDA: the same constructor parameters,
+    ``Init``, ``shader`` and LUT layouts; the LUTs are device buffers."""
+
+    kLambdaR = kLambdaR
+    kLambdaG = kLambdaG
+    kLambdaB = kLambdaB
+
+    def __init__(self, wavelengths, solar_irradiance, sun_angular_radius, bottom_radius,
+                 top_radius, rayleigh_density, rayleigh_scattering, mie_density,
+                 mie_scattering, mie_extinction, mie_phase_function_g, absorption_density,
+                 absorption_extinction, ground_albedo, max_sun_zenith_angle,
+                 length_unit_in_meters, num_precomputed_wavelengths,
+                 combine_scattering_textures, half_precision, lut_shape=None):
+        L = lib()
+        n = len(wavelengths)
+        self._keep = [np.ascontiguousarray(x, np.float64) for x in (
+            wavelengths, solar_irradiance, rayleigh_scattering, mie_scattering,
+            mie_extinction, absorption_extinction, ground_albedo)]
+        for arr in self._keep:
+            if arr.shape != (n,):
+                raise ValueError("spectral arrays must have len(wavelengths) entries")
+        ray, nr = _layers(rayleigh_density)
+        mie, nm = _layers(mie_density)
+        ab, na = _layers(absorption_density)
+        self._layers = (ray, mie, ab)
+        pp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        w, sol, rs, ms, me, ae, ga = self._keep
+        p = _ModelParams(pp(w), n, pp(sol), sun_angular_radius, bottom_radius, top_radius,
+                         ray, nr, pp(rs), mie, nm, pp(ms), pp(me), mie_phase_function_g,
+                         ab, na, pp(ae), pp(ga), max_sun_zenith_angle, length_unit_in_meters,
+                         num_precomputed_wavelengths, int(bool(combine_scattering_textures)),
+                         int(bool(half_precision)))
+        self._shape = LutShape.of(lut_shape) or LutShape(*DEFAULT_SHAPE)
+        self.combine_scattering_textures = bool(combine_scattering_textures)
+        self.half_precision = bool(half_precision)
+        self.num_precomputed_wavelengths = num_precomputed_wavelengths
+        h = C.c_void_p()
+        _check(L.atmo_model_create(C.byref(p), C.byref(self._shape), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.atmo_model_destroy(h)
+            self._h = None
+
+    # --- precomputation -------------------------------------------------------
+    def Init(self, num_scattering_orders=4, stream=None, path=None, synchronize=True):
+        """atmosphere/model.cc:866-975 on the GPU."""
+        if path is not None:
+            _check(lib().atmo_model_set_path(self._h, path))
+        _check(lib().atmo_model_init(self._h, num_scattering_orders, _stream_ptr(stream)))
+        if synchronize:
+            synchronize_stream(stream)
+
+    init = Init
+
+    def set_exact_parameters(self, exact=True):
+        _check(lib().atmo_model_set_exact_parameters(self._h, int(bool(exact))))
+
+    # --- LUT access -----------------------------------------------------------
+    def lut_view(self, kind) -> LutView:
+        v = LutView()
+        _check(lib().atmo_model_get_lut(self._h, kind, C.byref(v)))
+        return v
+
+    def _read(self, kind):
+        v = self.lut_view(kind)
+        out = np.empty((v.depth, v.height, v.width, 4), np.float32)
+        _check(lib().atmo_model_read_lut(self._h, kind,
+                                         out.ctypes.data_as(C.POINTER(C.c_float)), out.nbytes))
+        return out if v.depth > 1 else out[0]
+
+    def transmittance(self):
+        return self._read(LUT_TRANSMITTANCE)
+
+    def scattering(self):
+        return self._read(LUT_SCATTERING)
+
+    def single_mie_scattering(self):
+        return self._read(LUT_SINGLE_MIE)
+
+    def irradiance(self):
+        return self._read(LUT_IRRADIANCE)
+
+    def atmosphere_at(self, lambdas=(kLambdaR, kLambdaG, kLambdaB)) -> Atmosphere:
+        a = Atmosphere()
+        _check(lib().atmo_model_atmosphere_at(self._h, _dptr(lambdas), C.byref(a)))
+        return a
+
+    def luminance_factors(self):
+        sky, sun = (C.c_double * 3)(), (C.c_double * 3)()
+        _check(lib().atmo_model_luminance_factors(self._h, sky, sun))
+        return tuple(sky), tuple(sun)
+
+    def shader(self) -> str:
+        """The GLSL source the reference's shader() compiles (header of
+        atmosphere/model.cc:691-744 + API functions); the reference's own
+        definitions/functions.glsl text is not bundled and is marked."""
+        need = C.c_size_t()
+        _check(lib().atmo_model_shader_source(self._h, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        _check(lib().atmo_model_shader_source(self._h, buf, need.value, C.byref(need)))
+        return buf.value.decode()
+
+    def SetProgramUniforms(self, program, transmittance_texture_unit, scattering_texture_unit,
+                           irradiance_texture_unit, single_mie_scattering_texture_unit=0):
+        _check(lib().atmo_model_set_program_uniforms(
+            self._h, program, transmittance_texture_unit, scattering_texture_unit,
+            irradiance_texture_unit, single_mie_scattering_texture_unit))
+
+    @staticmethod
+    def ConvertSpectrumToLinearSrgb(wavelengths, spectrum):
+        """atmosphere/model.cc:1020-1040; returns (r, g, b)."""
+        r, g, b = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().atmo_convert_spectrum_to_linear_srgb(
+            _dptr(wavelengths), _dptr(spectrum), len(wavelengths), C.byref(r), C.byref(g),
+            C.byref(b)))
+        return r.value, g.value, b.value
+
+
+def measure_fp32_peak():
+    """This GPU's FP32 FMA throughput in TFLOP/s (2 FLOP per FMA)."""
+    t = C.c_double()
+    _check(lib().atmo_measure_fp32_peak(C.byref(t)))
+    return t.value
+
+
+def synchronize_stream(stream=None):
+    """Waits for the work enqueued on `stream` (None: the default stream)."""
+    _check(lib().atmo_synchronize(_stream_ptr(stream)))
+
+
+class Batch:
+    """Many independent atmospheres (uneven LUT shapes and order counts)
+    precomputed together; the pass sequence replays as a CUDA graph."""
+
+    def __init__(self, atmospheres, shapes=None, orders=4, combined=True):
+        n = len(atmospheres)
+        self.n = n
+        self._atm = (Atmosphere * n)(*[Atmosphere.from_buffer_of(a) for a in atmospheres])
+        if shapes is None:
+            shapes = [DEFAULT_SHAPE] * n
+        self.shapes = [LutShape.of(s) for s in shapes]
+        self._shapes = (LutShape * n)(*self.shapes)
+        if isinstance(orders, int):
+            orders = [orders] * n
+        self.orders = list(orders)
+        self._orders = (C.c_uint * n)(*self.orders)
+        self.combined = combined
+        h = C.c_void_p()
+        _check(lib().atmo_batch_create(self._atm, self._shapes, self._orders, n,
+                                       int(bool(combined)), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.atmo_batch_destroy(h)
+            self._h = None
+
+    def set_atmosphere(self, i, atmosphere):
+        a = Atmosphere.from_buffer_of(atmosphere)
+        _check(lib().atmo_batch_set_atmosphere(self._h, i, C.byref(a)))
+
+    def run(self, stream=None):
+        _check(lib().atmo_batch_run(self._h, _stream_ptr(stream)))
+
+    def kernel_count(self):
+        c = C.c_uint()
+        _check(lib().atmo_batch_kernel_count(self._h, C.byref(c)))
+        return c.value
+
+    PASS_NAMES = ("tables", "transmittance", "direct_irradiance", "single_scattering",
+                  "scattering_density", "indirect_irradiance", "multiple_scattering",
+                  "to_half")
+
+    def time_passes(self, stream=None):
+        """[(pass name, order, ms)] of one non-graph run, CUDA-event timed."""
+        cap = 4096
+        ms, ps, od = (C.c_float * cap)(), (C.c_int * cap)(), (C.c_int * cap)()
+        n = C.c_uint()
+        _check(lib().atmo_batch_time_passes(self._h, _stream_ptr(stream), cap, ms, ps, od,
+                                            C.byref(n)))
+        return [(self.PASS_NAMES[ps[i]], od[i], ms[i]) for i in range(min(n.value, cap))]
+
+    def lut_view(self, i, kind) -> LutView:
+        v = LutView()
+        _check(lib().atmo_batch_get_lut(self._h, i, kind, C.byref(v)))
+        return v
+
+    def read(self, i, kind):
+        v = self.lut_view(i, kind)
+        out = np.empty((v.depth, v.height, v.width, 4), np.float32)
+        _check(lib().atmo_batch_read_lut(self._h, i, kind,
+                                         out.ctypes.data_as(C.POINTER(C.c_float)), out.nbytes))
+        return out if v.depth > 1 else out[0]
+
+
+def precompute(atmosphere, shape, num_scattering_orders, transmittance, scattering, single_mie,
+               irradiance, lum=None, blend=False, combined=True, path=PATH_FAST, stream=None):
+    """One Model::Precompute group (atmosphere/model.cc:1048-1215) into
+    caller-owned float32 RGBA device buffers (device pointers as ints, or
+    objects with data_ptr())."""
+    a = Atmosphere.from_buffer_of(atmosphere)
+    s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+    lum_arr = None
+    if lum is not None:
+        lum_arr = (C.c_float * 9)(*[float(x) for x in np.asarray(lum).reshape(9)])
+    ptr = lambda t: None if t is None else (t if isinstance(t, int) else t.data_ptr())  # noqa
+    _check(lib().atmo_precompute(C.byref(a), C.byref(s), num_scattering_orders, lum_arr,
+                                 int(bool(blend)), int(bool(combined)), path, ptr(transmittance),
+                                 ptr(scattering), ptr(single_mie), ptr(irradiance),
+                                 _stream_ptr(stream)))

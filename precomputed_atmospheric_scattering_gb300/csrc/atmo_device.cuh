@@ -1,0 +1,430 @@
+// atmo_device.cuh -- device-side data layout and FP32 physics for the atmosphere
+// LUT precomputation (GB300, sm_103a).
+//
+// The functions here compute what atmosphere/functions.glsl:113-1601 of
+// ebruneton/precomputed_atmospheric_scattering computes, re-derived for FP32:
+// every ray-sphere quantity is carried as (rho, r, r*mu) with rho^2 = r^2 - Rb^2,
+// so that the cancellations of the reference's r^2(mu^2-1)+R^2 discriminants
+// become products of well-conditioned factors ((H - rho)(H + rho), (a - b)(a + b)).
+// Per-texel (r, mu, mu_s, nu) come from FP64 set-up tables (atmo_tables.cu), as
+// the reference's FP64 CPU model computes them.
+//
+// Compiles with nvcc (device) and with a host C++ compiler, so the same FP32
+// arithmetic can be exercised on the CPU.
+#ifndef ATMO_DEVICE_CUH_
+#define ATMO_DEVICE_CUH_
+
+#include <math.h>
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#include <cuda_fp16.h>
+#define ATMO_HD __host__ __device__ __forceinline__
+#else
+#define ATMO_HD inline
+struct float4 { float x, y, z, w; };
+struct float2 { float x, y; };
+inline float4 make_float4(float a, float b, float c, float d) { return float4{a, b, c, d}; }
+inline float2 make_float2(float a, float b) { return float2{a, b}; }
+inline float rsqrtf(float x) { return 1.0f / sqrtf(x); }
+#endif
+
+namespace atmo {
+
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr double kPiD = 3.14159265358979323846;
+// Quadrature sizes of the reference (functions.glsl:285, :704, :1190, :1486).
+constexpr int kOpticalLengthSamples = 500;
+constexpr int kSingleScatteringSamples = 50;
+constexpr int kMultipleScatteringSamples = 50;
+constexpr int kDensityThetaSamples = 16;    // 16 theta x 32 phi over the sphere
+constexpr int kDensityPhiSamples = 32;
+constexpr int kIndirectThetaSamples = 16;   // 16 theta x 64 phi over the hemisphere
+constexpr int kIndirectPhiSamples = 64;
+
+// ---------------------------------------------------------------------------
+// 3-wavelength spectra.
+// ---------------------------------------------------------------------------
+struct F3 {
+  float x, y, z;
+};
+ATMO_HD F3 f3(float a) { return F3{a, a, a}; }
+ATMO_HD F3 f3(float a, float b, float c) { return F3{a, b, c}; }
+ATMO_HD F3 f3(const float4& v) { return F3{v.x, v.y, v.z}; }
+ATMO_HD F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+ATMO_HD F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+ATMO_HD F3 operator*(F3 a, F3 b) { return F3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+ATMO_HD F3 operator/(F3 a, F3 b) { return F3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+ATMO_HD F3 operator*(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+ATMO_HD F3 operator*(float s, F3 a) { return F3{a.x * s, a.y * s, a.z * s}; }
+ATMO_HD F3& operator+=(F3& a, F3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+ATMO_HD F3 fma3(F3 a, float s, F3 c) {
+  return F3{fmaf(a.x, s, c.x), fmaf(a.y, s, c.y), fmaf(a.z, s, c.z)};
+}
+ATMO_HD F3 fma3(F3 a, F3 b, F3 c) {
+  return F3{fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z)};
+}
+ATMO_HD F3 min3(F3 a, float m) { return F3{fminf(a.x, m), fminf(a.y, m), fminf(a.z, m)}; }
+ATMO_HD F3 exp3(F3 a) { return F3{expf(a.x), expf(a.y), expf(a.z)}; }
+ATMO_HD float4 to4(F3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+ATMO_HD float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+// GLSL smoothstep; for the degenerate e0 == e1 (a point sun) it returns 0 at
+// x <= e0 and 1 above.
+ATMO_HD float smoothstepf(float e0, float e1, float x) {
+  if (x <= e0) return 0.0f;
+  if (x >= e1) return 1.0f;
+  float t = (x - e0) / (e1 - e0);
+  return t * t * (3.0f - 2.0f * t);
+}
+
+// ---------------------------------------------------------------------------
+// Per-instance constants (atmosphere/definitions.glsl:205-255 + derived).
+// ---------------------------------------------------------------------------
+struct LayerF {
+  float width, exp_term, exp_scale, linear_term, constant_term;
+};
+struct ProfileF {
+  LayerF layer[2];
+};
+
+struct Shape {
+  int tw, th;             // transmittance W x H
+  int sr, smu, smus, snu; // scattering R, MU, MU_S, NU
+  int iw, ih;             // irradiance W x H
+  ATMO_HD int sw() const { return snu * smus; }
+  ATMO_HD long long s_texels() const { return (long long)snu * smus * smu * sr; }
+  ATMO_HD int t_texels() const { return tw * th; }
+  ATMO_HD int i_texels() const { return iw * ih; }
+};
+
+struct Consts {
+  F3 solar, rayleigh, mie_sca, mie_ext, absorption, albedo;
+  ProfileF prof_r, prof_m, prof_a;
+  float mie_g, alpha_s;       // Mie g, sun angular radius
+  float Rb, Rt, H;            // bottom/top radius, H = sqrt(Rt^2 - Rb^2)
+  float mus_A;                // A of the mu_s mapping (functions.glsl:823-824)
+  float ray_k, mie_k;         // 3/(16 pi); 3/(8 pi)(1-g^2)/(2+g^2)
+  float g2p1, m2g;            // 1+g^2, -2g
+  float lum[9];               // luminance_from_radiance, row major
+  // FP64 copies for the set-up tables.
+  double dRb, dRt, dH, dmus_min, dA;
+};
+
+ATMO_HD float LayerDensity(const LayerF& l, float h) {
+  // functions.glsl:263-267
+  float d = l.exp_term * expf(l.exp_scale * h) + l.linear_term * h + l.constant_term;
+  return clampf(d, 0.0f, 1.0f);
+}
+ATMO_HD float ProfileDensity(const ProfileF& p, float h) {
+  // functions.glsl:269-273
+  return h < p.layer[0].width ? LayerDensity(p.layer[0], h) : LayerDensity(p.layer[1], h);
+}
+
+ATMO_HD float TexCoordFromUnitRange(float x, int n) {
+  // functions.glsl:342-344
+  return 0.5f / float(n) + x * (1.0f - 1.0f / float(n));
+}
+
+// A point on a ray: rho^2 = r^2 - Rb^2 kept separately from r so that the
+// altitude r - Rb = rho^2 / (r + Rb) keeps its relative precision.
+struct RadialPoint {
+  float rho, r, h;
+};
+ATMO_HD RadialPoint PointFromRho2(const Consts& c, float rho2) {
+  rho2 = clampf(rho2, 0.0f, c.H * c.H);
+  RadialPoint p;
+  p.rho = sqrtf(rho2);
+  p.r = sqrtf(rho2 + c.Rb * c.Rb);
+  p.h = rho2 / (p.r + c.Rb);
+  return p;
+}
+// Point at distance d along the ray (rho, r*mu): rho_d^2 = d^2 + 2 r mu d + rho^2.
+ATMO_HD RadialPoint PointAlongRay(const Consts& c, float rho, float rmu, float d) {
+  return PointFromRho2(c, fmaf(d, d + 2.0f * rmu, rho * rho));
+}
+
+// ---------------------------------------------------------------------------
+// Transmittance LUT (functions.glsl:402-421 mapping, :473-480 lookup).
+// ---------------------------------------------------------------------------
+// Distance to the top boundary from (rho, r) along r*mu:
+// -r mu + sqrt(H^2 - rho^2 + (r mu)^2), in its cancellation-free form.
+ATMO_HD float DistanceToTop(const Consts& c, float rho, float rmu) {
+  float hm = (c.H - rho) * (c.H + rho);
+  float sq = sqrtf(fmaxf(fmaf(rmu, rmu, hm), 0.0f));
+  return rmu > 0.0f ? hm / (rmu + sq) : sq - rmu;
+}
+
+ATMO_HD float2 TransmittanceUv(const Consts& c, const Shape& s, float rho, float r, float rmu) {
+  float hm = (c.H - rho) * (c.H + rho);
+  float d = DistanceToTop(c, rho, rmu);
+  float d_min = hm / (c.Rt + r);
+  float d_max = rho + c.H;
+  float x_mu = (d - d_min) / (d_max - d_min);
+  float x_r = rho / c.H;
+  return make_float2(TexCoordFromUnitRange(x_mu, s.tw), TexCoordFromUnitRange(x_r, s.th));
+}
+
+// GL LINEAR + CLAMP_TO_EDGE bilinear fetch of RGB from a float4 2D texture.
+ATMO_HD F3 Bilinear(const float4* __restrict__ tex, int w, int h, float u, float v) {
+  float x = u * float(w) - 0.5f, y = v * float(h) - 0.5f;
+  float fx = floorf(x), fy = floorf(y);
+  float a = x - fx, b = y - fy;
+  int i0 = (int)fx, j0 = (int)fy;
+  int i1 = i0 + 1, j1 = j0 + 1;
+  i0 = i0 < 0 ? 0 : (i0 > w - 1 ? w - 1 : i0);
+  i1 = i1 < 0 ? 0 : (i1 > w - 1 ? w - 1 : i1);
+  j0 = j0 < 0 ? 0 : (j0 > h - 1 ? h - 1 : j0);
+  j1 = j1 < 0 ? 0 : (j1 > h - 1 ? h - 1 : j1);
+#ifdef __CUDA_ARCH__
+  float4 t00 = __ldg(tex + j0 * w + i0), t10 = __ldg(tex + j0 * w + i1);
+  float4 t01 = __ldg(tex + j1 * w + i0), t11 = __ldg(tex + j1 * w + i1);
+#else
+  float4 t00 = tex[j0 * w + i0], t10 = tex[j0 * w + i1];
+  float4 t01 = tex[j1 * w + i0], t11 = tex[j1 * w + i1];
+#endif
+  float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
+  float w01 = (1.0f - a) * b, w11 = a * b;
+  return F3{t00.x * w00 + t10.x * w10 + t01.x * w01 + t11.x * w11,
+            t00.y * w00 + t10.y * w10 + t01.y * w01 + t11.y * w11,
+            t00.z * w00 + t10.z * w10 + t01.z * w01 + t11.z * w11};
+}
+
+ATMO_HD F3 TransmittanceToTop(const Consts& c, const Shape& s, const float4* T, float rho,
+                              float r, float rmu) {
+  float2 uv = TransmittanceUv(c, s, rho, r, rmu);
+  return Bilinear(T, s.tw, s.th, uv.x, uv.y);
+}
+
+// GetTransmittance (functions.glsl:493-515) for the segment of length d from
+// (rho, r, rmu); t_start is TransmittanceToTop at the start point in the
+// direction the reference uses (-mu when the ray hits the ground).
+ATMO_HD F3 SegmentTransmittance(const Consts& c, const Shape& s, const float4* T, float rmu,
+                                const RadialPoint& pd, float d, bool ground, F3 t_start) {
+  float rmu_d = clampf(rmu + d, -pd.r, pd.r);
+  if (ground) {
+    return min3(TransmittanceToTop(c, s, T, pd.rho, pd.r, -rmu_d) / t_start, 1.0f);
+  }
+  return min3(t_start / TransmittanceToTop(c, s, T, pd.rho, pd.r, rmu_d), 1.0f);
+}
+
+// GetTransmittanceToSun (functions.glsl:552-563) at point p with r*mu_s = rmu_s.
+ATMO_HD F3 TransmittanceToSun(const Consts& c, const Shape& s, const float4* T,
+                              const RadialPoint& p, float rmu_s) {
+  rmu_s = clampf(rmu_s, -p.r, p.r);
+  float sin_theta_h = c.Rb / p.r;
+  // mu_s - cos(theta_h) with cos(theta_h) = -rho / r.
+  float x = (rmu_s + p.rho) / p.r;
+  float e = sin_theta_h * c.alpha_s;
+  return TransmittanceToTop(c, s, T, p.rho, p.r, rmu_s) * smoothstepf(-e, e, x);
+}
+
+// ---------------------------------------------------------------------------
+// Scattering LUT mapping (functions.glsl:773-831) and 4D lookup (:958-976).
+// ---------------------------------------------------------------------------
+ATMO_HD float UMuSFromMuS(const Consts& c, const Shape& s, float mu_s) {
+  // d = DistanceToTopAtmosphereBoundary(Rb, mu_s), cancellation-free.
+  float rmus = c.Rb * mu_s;
+  float sq = sqrtf(fmaf(rmus, rmus, c.H * c.H));
+  float d = rmus > 0.0f ? (c.H * c.H) / (rmus + sq) : sq - rmus;
+  float d_min = c.Rt - c.Rb, d_max = c.H;
+  float a = (d - d_min) / (d_max - d_min);
+  return TexCoordFromUnitRange(fmaxf(1.0f - a / c.mus_A, 0.0f) / (1.0f + a), s.smus);
+}
+
+// u_mu when the distance to the ray's boundary is known (d_ray).
+ATMO_HD float UMuFromDistance(const Consts& c, const Shape& s, const RadialPoint& p,
+                              float d_ray, bool ground) {
+  int half = s.smu / 2;
+  if (ground) {
+    float d_min = p.h, d_max = p.rho;
+    float x = d_max == d_min ? 0.0f : clampf((d_ray - d_min) / (d_max - d_min), 0.0f, 1.0f);
+    return 0.5f - 0.5f * TexCoordFromUnitRange(x, half);
+  }
+  float d_min = (c.H - p.rho) * (c.H + p.rho) / (c.Rt + p.r);
+  float d_max = p.rho + c.H;
+  float x = clampf((d_ray - d_min) / (d_max - d_min), 0.0f, 1.0f);
+  return 0.5f + 0.5f * TexCoordFromUnitRange(x, half);
+}
+
+// u_mu from (rho, r*mu) alone (distance to the ground or to the top).
+ATMO_HD float UMuFromRMu(const Consts& c, const Shape& s, const RadialPoint& p, float rmu,
+                         bool ground) {
+  float d;
+  if (ground) {
+    // -r mu - sqrt((r mu)^2 - rho^2) = rho^2 / (-r mu + sqrt(...)).
+    float disc = fmaxf((rmu - p.rho) * (rmu + p.rho), 0.0f);
+    float den = sqrtf(disc) - rmu;
+    d = den > 0.0f ? p.rho * p.rho / den : 0.0f;
+  } else {
+    d = DistanceToTop(c, p.rho, rmu);
+  }
+  return UMuFromDistance(c, s, p, d, ground);
+}
+
+// Coordinates of one 4D lookup: the x texel column of the two nu nodes, the
+// nu lerp, and the fractional (y, z) position.
+struct Lookup4 {
+  float x0, x1;     // x coordinate in texels (before -0.5) of the two nu nodes
+  float lerp_nu;
+  float y, z;       // y, z texel coordinates (after -0.5)
+};
+ATMO_HD Lookup4 MakeLookup(const Shape& s, float u_nu, float u_mu_s, float u_mu, float u_r) {
+  Lookup4 L;
+  float tex_coord_x = u_nu * float(s.snu - 1);
+  float tex_x = floorf(tex_coord_x);
+  L.lerp_nu = tex_coord_x - tex_x;
+  L.x0 = (tex_x + u_mu_s) / float(s.snu) * float(s.sw()) - 0.5f;
+  L.x1 = (tex_x + 1.0f + u_mu_s) / float(s.snu) * float(s.sw()) - 0.5f;
+  L.y = u_mu * float(s.smu) - 0.5f;
+  L.z = u_r * float(s.sr) - 0.5f;
+  return L;
+}
+
+ATMO_HD int ClampIdx(int i, int n) { return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); }
+
+ATMO_HD F3 Trilinear(const float4* __restrict__ tex, const Shape& s, float x, float y,
+                     float z) {
+  const int W = s.sw(), Hh = s.smu, D = s.sr;
+  float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+  float a = x - fx, b = y - fy, cc = z - fz;
+  int i0 = ClampIdx((int)fx, W), i1 = ClampIdx((int)fx + 1, W);
+  int j0 = ClampIdx((int)fy, Hh), j1 = ClampIdx((int)fy + 1, Hh);
+  int k0 = ClampIdx((int)fz, D), k1 = ClampIdx((int)fz + 1, D);
+  F3 acc = f3(0.0f);
+  const int ii[2] = {i0, i1}, jj[2] = {j0, j1}, kk[2] = {k0, k1};
+  const float wi[2] = {1.0f - a, a}, wj[2] = {1.0f - b, b}, wk[2] = {1.0f - cc, cc};
+#pragma unroll
+  for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+    for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+      for (int di = 0; di < 2; ++di) {
+        long long idx = ((long long)kk[dk] * Hh + jj[dj]) * W + ii[di];
+#ifdef __CUDA_ARCH__
+        float4 t = __ldg(tex + idx);
+#else
+        float4 t = tex[idx];
+#endif
+        acc = fma3(f3(t), wi[di] * wj[dj] * wk[dk], acc);
+      }
+  return acc;
+}
+
+ATMO_HD F3 Scattering4(const float4* tex, const Shape& s, const Lookup4& L) {
+  F3 a = Trilinear(tex, s, L.x0, L.y, L.z);
+  F3 b = Trilinear(tex, s, L.x1, L.y, L.z);
+  return a * (1.0f - L.lerp_nu) + b * L.lerp_nu;
+}
+
+// functions.glsl:739-747
+ATMO_HD float RayleighPhase(const Consts& c, float nu) { return c.ray_k * (1.0f + nu * nu); }
+ATMO_HD float MiePhase(const Consts& c, float nu) {
+  float t = fmaf(c.m2g, nu, c.g2p1);
+  float rs = rsqrtf(t);
+  return c.mie_k * (1.0f + nu * nu) * (rs * rs * rs);
+}
+
+// ---------------------------------------------------------------------------
+// Irradiance LUT (functions.glsl:1524-1533, :1595-1601).
+// ---------------------------------------------------------------------------
+ATMO_HD F3 Irradiance(const Consts& c, const Shape& s, const float4* I, float h, float mu_s) {
+  float x_r = h / (c.Rt - c.Rb);
+  float x_mu_s = mu_s * 0.5f + 0.5f;
+  return Bilinear(I, s.iw, s.ih, TexCoordFromUnitRange(x_mu_s, s.iw),
+                  TexCoordFromUnitRange(x_r, s.ih));
+}
+
+ATMO_HD F3 MatVec(const float m[9], F3 v) {
+  return F3{m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+            m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+
+// ---------------------------------------------------------------------------
+// FP64 set-up tables: per scattering texel row / column, computed once per
+// precomputation by atmo_tables.cu with the reference's own double formulas.
+// ---------------------------------------------------------------------------
+struct TexelRow {        // one (r-slice k, mu-row j) of the scattering LUT
+  float r, rho, h;       // r, sqrt(r^2 - Rb^2), r - Rb
+  float mu, rmu;         // mu and r*mu of the row
+  float d;               // distance to the ray's boundary (ground or top)
+  float omega_x;         // sqrt(1 - mu^2)
+  float q;               // ground: sqrt((r mu)^2 - rho^2); else rho^2 - (r mu)^2 (>= 0)
+  int ground;            // ray_r_mu_intersects_ground
+  int pad[3];
+};
+
+// rho^2 at distance t along the texel row's ray, where e = row.d - t is the
+// distance left to the ray's end (passed separately so that it is exactly 0
+// at the last quadrature sample), written so that no form cancels: for a
+// ground ray e (e + 2q) vanishes exactly at the ground point; for an upward
+// ray t (t + 2 r mu) + rho^2 adds non-negative terms; for a downward ray that
+// misses the ground (t + r mu)^2 + q adds non-negative terms.
+ATMO_HD float RayRho2(const TexelRow& row, float t, float e) {
+  if (row.ground) return e * (e + 2.0f * row.q);
+  if (row.rmu >= 0.0f) return fmaf(t, t + 2.0f * row.rmu, row.rho * row.rho);
+  float u = t + row.rmu;
+  return fmaf(u, u, row.q);
+}
+struct TexelCol {        // one mu_s column c
+  float mu_s, sin_s;     // mu_s, sqrt(1 - mu_s^2)
+  float u_mu_s;          // forward-mapped texture coordinate of mu_s
+  float pad;
+};
+struct DensityRow {      // one (r-slice k, theta sample l) of the density integral
+  float cos_t, sin_t;    // cos/sin of theta_l
+  float dist_ground;     // distance to the ground (0 when the ray misses it)
+  int ground;            // RayIntersectsGround(r, cos theta_l)
+  float u_mu;            // texture coordinate of (r, cos theta_l)
+  float pad0, pad1, pad2;
+  float4 t_ground;       // transmittance to the ground x albedo / pi
+};
+
+struct IrrRow {          // one r row of the irradiance LUT
+  float r, rho, h, pad;
+};
+
+struct Tables {
+  TexelRow* rows;        // [sr * smu]
+  TexelCol* cols;        // [smus]
+  DensityRow* drows;     // [sr * 16]
+  IrrRow* irows;         // [ih]
+  float* mus_i;          // [iw] mu_s of the irradiance columns
+};
+
+// Texel (x, y, z) of the scattering LUT -> (row, column, nu node).
+ATMO_HD void SplitTexel(const Shape& s, long long idx, int* k, int* j, int* c, int* n) {
+  int W = s.sw();
+  int x = (int)(idx % W);
+  long long yz = idx / W;
+  *j = (int)(yz % s.smu);
+  *k = (int)(yz / s.smu);
+  *n = x / s.smus;
+  *c = x % s.smus;
+}
+
+// The texel's nu after the clamp of functions.glsl:924-925, and the sun
+// direction of functions.glsl:1176-1180 (omega_s = (sx, sy, mu_s)).
+struct TexelAngles {
+  float mu, mu_s, nu, omega_x, sx, sy;
+};
+ATMO_HD TexelAngles MakeAngles(const Shape& s, const TexelRow& row, const TexelCol& col,
+                               int n) {
+  TexelAngles a;
+  a.mu = row.mu;
+  a.mu_s = col.mu_s;
+  a.omega_x = row.omega_x;
+  float nu_g = clampf(float(n) / float(s.snu - 1) * 2.0f - 1.0f, -1.0f, 1.0f);
+  float mm = row.mu * col.mu_s;
+  float lim = row.omega_x * col.sin_s;   // sqrt((1 - mu^2)(1 - mu_s^2))
+  float t = clampf(nu_g - mm, -lim, lim);
+  a.nu = mm + t;
+  a.sx = row.omega_x == 0.0f ? 0.0f : clampf(t / row.omega_x, -col.sin_s, col.sin_s);
+  float ax = fabsf(a.sx);
+  a.sy = sqrtf(fmaxf((col.sin_s - ax) * (col.sin_s + ax), 0.0f));
+  return a;
+}
+
+}  // namespace atmo
+
+#endif  // ATMO_DEVICE_CUH_

@@ -1,0 +1,36 @@
+// atmo_kernels.h -- launchers of the precomputation kernels (host side).
+#ifndef ATMO_KERNELS_H_
+#define ATMO_KERNELS_H_
+
+#include <cuda_runtime.h>
+
+#include "atmo_instance.h"
+
+namespace atmo {
+
+int TableTiles(const Shape& s);
+cudaError_t LaunchTables(const Instance* insts, WorkList wl, int tiles, cudaStream_t st);
+cudaError_t LaunchTransmittance(const Instance* insts, WorkList wl, int tiles, cudaStream_t st);
+cudaError_t LaunchDirectIrradiance(const Instance* insts, WorkList wl, int tiles,
+                                   cudaStream_t st);
+cudaError_t LaunchSingleScattering(const Instance* insts, WorkList wl, int tiles,
+                                   cudaStream_t st);
+cudaError_t LaunchDensityPlain(const Instance* insts, WorkList wl, int tiles, int order,
+                               cudaStream_t st);
+cudaError_t LaunchIndirectIrradiance(const Instance* insts, WorkList wl, int tiles, int order,
+                                     cudaStream_t st);
+cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
+                                cudaStream_t st);
+// Fast path (atmo_fast.cu).
+int DensityFastTiles(const Shape& s);
+cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
+                              cudaStream_t st);
+cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles,
+                               cudaStream_t st);
+// Final conversion of the scattering accumulators to half precision.
+cudaError_t LaunchToHalf(const float4* src, void* dst, long long n, cudaStream_t st);
+cudaError_t MeasureFp32Peak(double* tflops);
+
+}  // namespace atmo
+
+#endif  // ATMO_KERNELS_H_

@@ -1,0 +1,295 @@
+// atmo_program.cu -- device storage and launch programs (see atmo_program.h).
+#include "atmo_program.h"
+
+#include <cstring>
+
+#include "atmo_kernels.h"
+#include "atmo_tables.cuh"
+
+namespace atmo {
+
+namespace {
+thread_local std::string g_last_error = "no error";
+}  // namespace
+
+void SetError(const std::string& msg) { g_last_error = msg; }
+const char* LastError() { return g_last_error.c_str(); }
+
+atmo_status CudaFail(cudaError_t e, const char* what) {
+  SetError(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+  return e == cudaErrorMemoryAllocation ? ATMO_OOM : ATMO_CUDA_ERROR;
+}
+
+// ---------------------------------------------------------------------------
+// Storage
+// ---------------------------------------------------------------------------
+atmo_status Storage::Allocate(const Shape& shape, bool combined_textures, bool half_precision) {
+  Free();
+  s = shape;
+  combined = combined_textures;
+  half = half_precision;
+  const size_t nT = (size_t)s.t_texels(), nI = (size_t)s.i_texels(),
+               nS = (size_t)s.s_texels();
+  auto alloc = [&](void** p, size_t bytes) -> atmo_status {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      Free();
+      return CudaFail(e, "cudaMalloc");
+    }
+    owned.push_back(*p);
+    return ATMO_OK;
+  };
+  atmo_status st;
+#define ATMO_ALLOC(ptr, bytes)                                   \
+  if ((st = alloc(reinterpret_cast<void**>(&(ptr)), (bytes))) != ATMO_OK) return st;
+  ATMO_ALLOC(T, nT * sizeof(float4));
+  ATMO_ALLOC(I, nI * sizeof(float4));
+  ATMO_ALLOC(dI, nI * sizeof(float4));
+  ATMO_ALLOC(dR, nS * sizeof(float4));
+  ATMO_ALLOC(dM, nS * sizeof(float4));
+  ATMO_ALLOC(dJ, nS * sizeof(float4));
+  ATMO_ALLOC(S, nS * sizeof(float4));
+  if (!combined) ATMO_ALLOC(M, nS * sizeof(float4));
+  if (half) {
+    ATMO_ALLOC(S_half, nS * 8);
+    if (!combined) ATMO_ALLOC(M_half, nS * 8);
+  }
+  ATMO_ALLOC(tab.rows, (size_t)s.sr * s.smu * sizeof(TexelRow));
+  ATMO_ALLOC(tab.cols, (size_t)s.smus * sizeof(TexelCol));
+  ATMO_ALLOC(tab.drows, (size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow));
+  ATMO_ALLOC(tab.irows, (size_t)s.ih * sizeof(IrrRow));
+  ATMO_ALLOC(tab.mus_i, (size_t)s.iw * sizeof(float));
+#undef ATMO_ALLOC
+  return ATMO_OK;
+}
+
+void Storage::Free() {
+  for (void* p : owned) cudaFree(p);
+  owned.clear();
+  T = I = dI = dR = dM = dJ = S = M = nullptr;
+  S_half = M_half = nullptr;
+  tab = Tables{};
+}
+
+size_t Storage::Bytes() const {
+  const size_t nT = (size_t)s.t_texels(), nI = (size_t)s.i_texels(),
+               nS = (size_t)s.s_texels();
+  size_t b = (nT + 2 * nI) * 16 + nS * 16 * (4 + (combined ? 0 : 1));
+  if (half) b += nS * 8 * (combined ? 1 : 2);
+  b += (size_t)s.sr * s.smu * sizeof(TexelRow) + s.smus * sizeof(TexelCol) +
+       (size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow) + s.ih * sizeof(IrrRow) +
+       s.iw * sizeof(float);
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Program
+// ---------------------------------------------------------------------------
+int Tiles(Pass pass, const Shape& s, atmo_path path) {
+  auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
+  switch (pass) {
+    case Pass::kTables: return TableTiles(s);
+    case Pass::kTransmittance: return cdiv(s.t_texels(), kTransmittanceTexelsPerTile);
+    case Pass::kDirect: return cdiv(s.i_texels() + s.sr * kDensityThetaSamples, kTexelThreads);
+    case Pass::kSingle: return cdiv(s.s_texels(), kTexelThreads);
+    case Pass::kDensity:
+      return path == ATMO_PATH_FAST ? DensityFastTiles(s) : cdiv(s.s_texels(), kTexelThreads);
+    case Pass::kIndirect: return cdiv(s.i_texels(), kIndirectTexelsPerTile);
+    case Pass::kMultiple: return cdiv(s.s_texels(), kTexelThreads);
+    case Pass::kToHalf: return cdiv(s.s_texels(), 256);
+  }
+  return 0;
+}
+
+Program::~Program() {
+  if (graph_) cudaGraphExecDestroy(graph_);
+  if (capture_stream_) cudaStreamDestroy(capture_stream_);
+  if (upload_done_) cudaEventDestroy(upload_done_);
+  if (d_slots_) cudaFree(d_slots_);
+  if (h_slots_pinned_) cudaFreeHost(h_slots_pinned_);
+  if (d_blob_) cudaFree(d_blob_);
+}
+
+int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles) {
+  std::vector<int> inst, start;
+  int t = 0;
+  for (int m : members) {
+    if ((pass == Pass::kDensity || pass == Pass::kMultiple) && orders[m] < (unsigned)order)
+      continue;
+    if (pass == Pass::kIndirect && orders[m] < (unsigned)order + 1) continue;
+    inst.push_back(m);
+    start.push_back(t);
+    t += Tiles(pass, slots[m].s, path);
+  }
+  *tiles = t;
+  if (inst.empty()) return -1;
+  start.push_back(t);
+  int offset = (int)blob_.size();
+  blob_.insert(blob_.end(), inst.begin(), inst.end());
+  blob_.insert(blob_.end(), start.begin(), start.end());
+  wl_offsets_.push_back({offset, (int)inst.size()});
+  return (int)wl_offsets_.size() - 1;
+}
+
+void Program::AddStage(const std::vector<int>& members, bool transmittance_only) {
+  auto add = [&](Pass p, int order) {
+    int tiles = 0;
+    int wl = AddWorkList(members, p, order, &tiles);
+    if (wl >= 0 && tiles > 0) steps_.push_back(Step{p, order, wl, tiles});
+  };
+  if (transmittance_only) {
+    add(Pass::kTransmittance, 0);
+    return;
+  }
+  unsigned max_order = 1;
+  for (int m : members) max_order = orders[m] > max_order ? orders[m] : max_order;
+  add(Pass::kTables, 0);
+  add(Pass::kTransmittance, 0);
+  add(Pass::kDirect, 0);
+  add(Pass::kSingle, 0);
+  for (unsigned order = 2; order <= max_order; ++order) {
+    add(Pass::kDensity, (int)order);
+    add(Pass::kIndirect, (int)order - 1);
+    add(Pass::kMultiple, (int)order);
+  }
+}
+
+void Program::AddToHalf(const std::vector<int>& members) {
+  for (int m : members) {
+    int tiles = 0;
+    int wl = AddWorkList({m}, Pass::kToHalf, 0, &tiles);
+    if (wl >= 0) steps_.push_back(Step{Pass::kToHalf, 0, wl, tiles});
+  }
+}
+
+atmo_status Program::Finalize() {
+  if (finalized_) return ATMO_OK;
+  if (!blob_.empty()) {
+    ATMO_CUDA_TRY(cudaMalloc(&d_blob_, blob_.size() * sizeof(int)));
+    ATMO_CUDA_TRY(cudaMemcpy(d_blob_, blob_.data(), blob_.size() * sizeof(int),
+                             cudaMemcpyHostToDevice));
+  }
+  wls_.clear();
+  for (auto& o : wl_offsets_) {
+    WorkList w;
+    w.inst = d_blob_ + o.first;
+    w.start = d_blob_ + o.first + o.second;
+    w.count = o.second;
+    wls_.push_back(w);
+  }
+  ATMO_CUDA_TRY(cudaMalloc(&d_slots_, slots.size() * sizeof(Instance)));
+  ATMO_CUDA_TRY(cudaMallocHost(&h_slots_pinned_, slots.size() * sizeof(Instance)));
+  finalized_ = true;
+  return ATMO_OK;
+}
+
+atmo_status Program::Upload(cudaStream_t st) {
+  if (!upload_done_) {
+    ATMO_CUDA_TRY(cudaEventCreateWithFlags(&upload_done_, cudaEventDisableTiming));
+  } else {
+    // The previous run's copy may still be reading the staging buffer.
+    ATMO_CUDA_TRY(cudaEventSynchronize(upload_done_));
+  }
+  std::memcpy(h_slots_pinned_, slots.data(), slots.size() * sizeof(Instance));
+  ATMO_CUDA_TRY(cudaMemcpyAsync(d_slots_, h_slots_pinned_, slots.size() * sizeof(Instance),
+                                cudaMemcpyHostToDevice, st));
+  ATMO_CUDA_TRY(cudaEventRecord(upload_done_, st));
+  return ATMO_OK;
+}
+
+atmo_status Program::Launch(cudaStream_t st) {
+  for (size_t i = 0; i < steps_.size(); ++i) {
+    atmo_status s = LaunchStep(i, st);
+    if (s != ATMO_OK) return s;
+  }
+  return ATMO_OK;
+}
+
+atmo_status Program::TimeSteps(cudaStream_t st, std::vector<float>* ms) {
+  atmo_status s = Finalize();
+  if (s != ATMO_OK) return s;
+  if ((s = Upload(st)) != ATMO_OK) return s;
+  std::vector<cudaEvent_t> ev(steps_.size() + 1);
+  for (auto& e : ev) ATMO_CUDA_TRY(cudaEventCreate(&e));
+  ATMO_CUDA_TRY(cudaEventRecord(ev[0], st));
+  for (size_t i = 0; i < steps_.size(); ++i) {
+    if ((s = LaunchStep(i, st)) != ATMO_OK) break;
+    ATMO_CUDA_TRY(cudaEventRecord(ev[i + 1], st));
+  }
+  cudaError_t e = cudaEventSynchronize(ev.back());
+  ms->assign(steps_.size(), 0.0f);
+  for (size_t i = 0; s == ATMO_OK && e == cudaSuccess && i < steps_.size(); ++i)
+    cudaEventElapsedTime(&(*ms)[i], ev[i], ev[i + 1]);
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (s != ATMO_OK) return s;
+  if (e != cudaSuccess) return CudaFail(e, "cudaEventSynchronize");
+  return ATMO_OK;
+}
+
+atmo_status Program::LaunchStep(size_t i, cudaStream_t st) {
+  {
+    const Step& step = steps_[i];
+    const WorkList& wl = wls_[step.wl];
+    cudaError_t e = cudaSuccess;
+    switch (step.pass) {
+      case Pass::kTables: e = LaunchTables(d_slots_, wl, step.tiles, st); break;
+      case Pass::kTransmittance: e = LaunchTransmittance(d_slots_, wl, step.tiles, st); break;
+      case Pass::kDirect: e = LaunchDirectIrradiance(d_slots_, wl, step.tiles, st); break;
+      case Pass::kSingle: e = LaunchSingleScattering(d_slots_, wl, step.tiles, st); break;
+      case Pass::kDensity:
+        e = path == ATMO_PATH_FAST ? LaunchDensityFast(d_slots_, wl, step.tiles, step.order, st)
+                                   : LaunchDensityPlain(d_slots_, wl, step.tiles, step.order, st);
+        break;
+      case Pass::kIndirect:
+        e = LaunchIndirectIrradiance(d_slots_, wl, step.tiles, step.order, st);
+        break;
+      case Pass::kMultiple:
+        e = path == ATMO_PATH_FAST ? LaunchMultipleFast(d_slots_, wl, step.tiles, st)
+                                   : LaunchMultiplePlain(d_slots_, wl, step.tiles, st);
+        break;
+      case Pass::kToHalf: {
+        // One slot per step: convert its scattering (and single-Mie) outputs.
+        int m = blob_[wl_offsets_[step.wl].first];
+        const Instance& in = slots[m];
+        if (in.S_half) e = LaunchToHalf(in.S, in.S_half, in.s.s_texels(), st);
+        if (e == cudaSuccess && in.M && in.M_half)
+          e = LaunchToHalf(in.M, in.M_half, in.s.s_texels(), st);
+        break;
+      }
+    }
+    if (e != cudaSuccess) return CudaFail(e, "kernel launch");
+  }
+  return ATMO_OK;
+}
+
+atmo_status Program::Run(cudaStream_t st, bool use_graph) {
+  atmo_status s = Finalize();
+  if (s != ATMO_OK) return s;
+  if ((s = Upload(st)) != ATMO_OK) return s;
+  if (!use_graph) return Launch(st);
+  if (!graph_) {
+    if (!capture_stream_) {
+      ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+    }
+    cudaGraph_t g = nullptr;
+    ATMO_CUDA_TRY(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
+    atmo_status ls = Launch(capture_stream_);
+    cudaError_t ce = cudaStreamEndCapture(capture_stream_, &g);
+    if (ls != ATMO_OK) {
+      if (g) cudaGraphDestroy(g);
+      return ls;
+    }
+    if (ce != cudaSuccess) return CudaFail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      graph_ = nullptr;
+      return CudaFail(ce, "cudaGraphInstantiate");
+    }
+  }
+  ATMO_CUDA_TRY(cudaGraphLaunch(graph_, st));
+  return ATMO_OK;
+}
+
+}  // namespace atmo

@@ -1,0 +1,66 @@
+"""Batched precomputation: many atmospheres with uneven LUT shapes and order
+counts in one pass sequence (CUDA graph).  Every instance must produce exactly
+the LUTs it produces alone, and agree with the oracle."""
+import numpy as np
+import pytest
+
+from parity import TOL_IRRADIANCE, TOL_SCATTERING, TOL_TRANSMITTANCE, check
+from test_gpu_parity import gpu_precompute, random_atmosphere
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+SHAPES = [(64, 16, 4, 16, 8, 4, 16, 4), (128, 32, 8, 32, 16, 8, 32, 8),
+          (32, 8, 2, 8, 4, 2, 8, 2), (64, 16, 6, 20, 8, 4, 16, 4)]
+
+
+def test_batch_uneven_equals_alone_and_oracle(atmo, oracle, torch):
+    rng = np.random.default_rng(99)
+    n = 6
+    atms = [random_atmosphere(oracle, rng) for _ in range(n)]
+    shapes = [SHAPES[i % len(SHAPES)] for i in range(n)]
+    orders = [int(rng.integers(2, 7)) for _ in range(n)]
+    b = atmo.Batch(atms, shapes, orders, combined=True)
+    b.run()
+    atmo.synchronize_stream()
+    for i in range(n):
+        T = b.read(i, atmo.LUT_TRANSMITTANCE)
+        S = b.read(i, atmo.LUT_SCATTERING)
+        I = b.read(i, atmo.LUT_IRRADIANCE)
+        alone = gpu_precompute(atmo, torch, atms[i], shapes[i], orders[i], True, 0)
+        np.testing.assert_array_equal(T, alone[0])
+        np.testing.assert_array_equal(S, alone[1])
+        np.testing.assert_array_equal(I, alone[3])
+        if i < 3:
+            ref = oracle.precompute(atms[i], shapes[i], orders[i], combined=True)
+            check("T", T, ref.transmittance, TOL_TRANSMITTANCE)
+            check("S", S, ref.scattering, TOL_SCATTERING, channels=4)
+            check("I", I, ref.irradiance, TOL_IRRADIANCE)
+
+
+def test_batch_replay_and_parameter_update(atmo, oracle, torch):
+    rng = np.random.default_rng(5)
+    atms = [random_atmosphere(oracle, rng) for _ in range(3)]
+    b = atmo.Batch(atms, [SHAPES[0]] * 3, [3, 4, 2])
+    b.run()
+    atmo.synchronize_stream()
+    s0 = b.read(1, atmo.LUT_SCATTERING)
+    b.run()
+    atmo.synchronize_stream()
+    np.testing.assert_array_equal(s0, b.read(1, atmo.LUT_SCATTERING))
+    new = random_atmosphere(oracle, rng)
+    new.bottom_radius, new.top_radius = atms[1].bottom_radius, atms[1].top_radius
+    b.set_atmosphere(1, new)
+    b.run()
+    atmo.synchronize_stream()
+    alone = gpu_precompute(atmo, torch, new, SHAPES[0], 4, True, 0)
+    np.testing.assert_array_equal(b.read(1, atmo.LUT_SCATTERING), alone[1])
+    assert b.kernel_count() > 0
