@@ -196,6 +196,7 @@ struct atmo_model {
     in.s = storage.s;
     in.tab = storage.tab;
     in.T = storage.T;
+    in.Tau = storage.Tau;
     in.I = storage.I;
     in.dI = storage.dI;
     in.dR = storage.dR;
@@ -619,13 +620,15 @@ atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_sh
   in.combined = combined ? 1 : 0;
   in.blend = blend ? 1 : 0;
   // Temporaries, stream ordered.
-  const size_t bytes[8] = {nI * 16, nS * 16, nS * 16, nS * 16,
+  const size_t nT = (size_t)s.t_texels();
+  const size_t bytes[9] = {nI * 16, nS * 16, nS * 16, nS * 16,
                            (size_t)s.sr * s.smu * sizeof(TexelRow),
                            (size_t)s.smus * sizeof(TexelCol),
                            (size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow),
-                           (size_t)s.ih * sizeof(IrrRow) + (size_t)s.iw * sizeof(float)};
-  void* tmp[8] = {nullptr};
-  for (int i = 0; i < 8; ++i) {
+                           (size_t)s.ih * sizeof(IrrRow) + (size_t)s.iw * sizeof(float),
+                           nT * 16};
+  void* tmp[9] = {nullptr};
+  for (int i = 0; i < 9; ++i) {
     cudaError_t e = cudaMallocAsync(&tmp[i], bytes[i], st);
     if (e != cudaSuccess) {
       for (int j = 0; j < i; ++j) cudaFreeAsync(tmp[j], st);
@@ -641,6 +644,7 @@ atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_sh
   in.tab.drows = (DensityRow*)tmp[6];
   in.tab.irows = (IrrRow*)tmp[7];
   in.tab.mus_i = (float*)((char*)tmp[7] + (size_t)s.ih * sizeof(IrrRow));
+  in.Tau = (float4*)tmp[8];
   atmo_status result;
   {
     Program prog;
@@ -654,7 +658,7 @@ atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_sh
     cudaError_t e = cudaStreamSynchronize(st);
     if (result == ATMO_OK && e != cudaSuccess) result = CudaFail(e, "precompute");
   }
-  for (int i = 0; i < 8; ++i) cudaFreeAsync(tmp[i], st);
+  for (int i = 0; i < 9; ++i) cudaFreeAsync(tmp[i], st);
   return result;
 }
 
@@ -692,6 +696,7 @@ atmo_status atmo_batch_create(const atmo_atmosphere* atmospheres, const atmo_lut
     in.s = sto.s;
     in.tab = sto.tab;
     in.T = sto.T;
+    in.Tau = sto.Tau;
     in.I = sto.I;
     in.dI = sto.dI;
     in.dR = sto.dR;

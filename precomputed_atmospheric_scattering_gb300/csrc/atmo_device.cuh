@@ -155,16 +155,6 @@ ATMO_HD float DistanceToTop(const Consts& c, float rho, float rmu) {
   return rmu > 0.0f ? hm / (rmu + sq) : sq - rmu;
 }
 
-ATMO_HD float2 TransmittanceUv(const Consts& c, const Shape& s, float rho, float r, float rmu) {
-  float hm = (c.H - rho) * (c.H + rho);
-  float d = DistanceToTop(c, rho, rmu);
-  float d_min = hm / (c.Rt + r);
-  float d_max = rho + c.H;
-  float x_mu = (d - d_min) / (d_max - d_min);
-  float x_r = rho / c.H;
-  return make_float2(TexCoordFromUnitRange(x_mu, s.tw), TexCoordFromUnitRange(x_r, s.th));
-}
-
 // GL LINEAR + CLAMP_TO_EDGE bilinear fetch of RGB from a float4 2D texture.
 ATMO_HD F3 Bilinear(const float4* __restrict__ tex, int w, int h, float u, float v) {
   float x = u * float(w) - 0.5f, y = v * float(h) - 0.5f;
@@ -190,22 +180,163 @@ ATMO_HD F3 Bilinear(const float4* __restrict__ tex, int w, int h, float u, float
             t00.z * w00 + t10.z * w10 + t01.z * w01 + t11.z * w11};
 }
 
+// Transmittance LUT lookup (the mapping of functions.glsl:402-421 and the
+// bilinear fetch of :473-480) for the ray from (rho, r) along r*mu = rmu.
+// delta = rho^2 - rmu^2 = p^2 - Rb^2 (p the ray's impact parameter) is passed
+// in because it is invariant along a ray and known accurately there; from it
+// 1 - x_mu = (d_max - d) / (d_max - d_min) is formed without cancellation:
+//   d_max - d = (rho + r mu) + (H - sqrt(H^2 - delta)),
+//   rho + r mu = delta / (rho - r mu) when r mu < 0,
+//   H - sqrt(H^2 - delta) = delta / (H + sqrt(H^2 - delta)),
+// so that rays grazing the ground (delta ~ 0, x_mu ~ 1), where neighbouring
+// texel columns can differ by orders of magnitude, keep their exact weights.
+struct TCoords {
+  int i00, i10, i01, i11;      // texel indices of the four taps
+  float w00, w10, w01, w11;    // bilinear weights
+};
+ATMO_HD TCoords TransmittanceCoords(const Consts& c, const Shape& s, float rho, float r,
+                                    float rmu, float delta) {
+  const float a = -rmu;
+  float sq = sqrtf(fmaxf(c.H * c.H - delta, 0.0f));
+  float rho_minus_a = a > 0.0f ? (rho + a > 0.0f ? delta / (rho + a) : 0.0f) : rho - a;
+  float dmax_minus_d = rho_minus_a + delta / (c.H + sq);
+  float d_min = (c.H - rho) * (c.H + rho) / (c.Rt + r);
+  float d_max = rho + c.H;
+  float omx = clampf(dmax_minus_d / (d_max - d_min), 0.0f, 1.0f);
+  // Texel coordinate X = x_mu (W - 1) = (W - 1) - Xc, fetched from the two
+  // columns below W - 1 - floor(Xc) with weights computed from Xc itself.
+  const int W = s.tw, Hh = s.th;
+  float Xc = omx * float(W - 1);
+  float f = floorf(Xc);
+  float g = Xc - f;                       // weight of the lower column
+  int i_hi = W - 1 - (int)f;
+  int i_lo = i_hi - 1;
+  i_hi = i_hi < 0 ? 0 : i_hi;
+  i_lo = i_lo < 0 ? 0 : i_lo;
+  float Y = rho / c.H * float(Hh - 1);
+  float fy = floorf(Y);
+  float b = Y - fy;
+  int j0 = (int)fy, j1 = j0 + 1;
+  j0 = j0 < 0 ? 0 : (j0 > Hh - 1 ? Hh - 1 : j0);
+  j1 = j1 < 0 ? 0 : (j1 > Hh - 1 ? Hh - 1 : j1);
+  TCoords t;
+  t.i00 = j0 * W + i_lo;
+  t.i10 = j0 * W + i_hi;
+  t.i01 = j1 * W + i_lo;
+  t.i11 = j1 * W + i_hi;
+  t.w00 = g * (1.0f - b);
+  t.w10 = (1.0f - g) * (1.0f - b);
+  t.w01 = g * b;
+  t.w11 = (1.0f - g) * b;
+  return t;
+}
+
+ATMO_HD float4 LoadTexel(const float4* __restrict__ tex, int i) {
+#ifdef __CUDA_ARCH__
+  return __ldg(tex + i);
+#else
+  return tex[i];
+#endif
+}
+
+ATMO_HD F3 FetchTransmittance(const float4* __restrict__ T, const TCoords& t) {
+  float4 a = LoadTexel(T, t.i00), b = LoadTexel(T, t.i10);
+  float4 c = LoadTexel(T, t.i01), d = LoadTexel(T, t.i11);
+  return F3{a.x * t.w00 + b.x * t.w10 + c.x * t.w01 + d.x * t.w11,
+            a.y * t.w00 + b.y * t.w10 + c.y * t.w01 + d.y * t.w11,
+            a.z * t.w00 + b.z * t.w10 + c.z * t.w01 + d.z * t.w11};
+}
+
+ATMO_HD F3 TransmittanceLookup(const Consts& c, const Shape& s, const float4* __restrict__ T,
+                               float rho, float r, float rmu, float delta) {
+  return FetchTransmittance(T, TransmittanceCoords(c, s, rho, r, rmu, delta));
+}
+
+// A transmittance lookup kept as m * exp(-e) per channel, from the optical
+// depth LUT (tau = -ln T): e = the smallest tau among the weighted taps and
+// m = sum_k w_k exp(e - tau_k) in (0, 1].  Ratios of two such values stay
+// accurate where the transmittance itself is below FP32's normal range.
+struct TExp {
+  F3 m, e;
+};
+ATMO_HD float MinTau(float a, float wa, float b, float wb, float c, float wc, float d,
+                     float wd) {
+  float m = 3.0e38f;
+  if (wa > 0.0f) m = fminf(m, a);
+  if (wb > 0.0f) m = fminf(m, b);
+  if (wc > 0.0f) m = fminf(m, c);
+  if (wd > 0.0f) m = fminf(m, d);
+  return m;
+}
+ATMO_HD TExp FetchTau(const float4* __restrict__ Tau, const TCoords& t) {
+  float4 a = LoadTexel(Tau, t.i00), b = LoadTexel(Tau, t.i10);
+  float4 c = LoadTexel(Tau, t.i01), d = LoadTexel(Tau, t.i11);
+  TExp r;
+  r.e.x = MinTau(a.x, t.w00, b.x, t.w10, c.x, t.w01, d.x, t.w11);
+  r.e.y = MinTau(a.y, t.w00, b.y, t.w10, c.y, t.w01, d.y, t.w11);
+  r.e.z = MinTau(a.z, t.w00, b.z, t.w10, c.z, t.w01, d.z, t.w11);
+  r.m.x = t.w00 * expf(r.e.x - a.x) + t.w10 * expf(r.e.x - b.x) + t.w01 * expf(r.e.x - c.x) +
+          t.w11 * expf(r.e.x - d.x);
+  r.m.y = t.w00 * expf(r.e.y - a.y) + t.w10 * expf(r.e.y - b.y) + t.w01 * expf(r.e.y - c.y) +
+          t.w11 * expf(r.e.y - d.y);
+  r.m.z = t.w00 * expf(r.e.z - a.z) + t.w10 * expf(r.e.z - b.z) + t.w01 * expf(r.e.z - c.z) +
+          t.w11 * expf(r.e.z - d.z);
+  return r;
+}
+// num / den for values in the m * exp(-e) form.
+ATMO_HD F3 TExpRatio(const TExp& num, const TExp& den) {
+  return F3{num.m.x / den.m.x * expf(den.e.x - num.e.x),
+            num.m.y / den.m.y * expf(den.e.y - num.e.y),
+            num.m.z / den.m.z * expf(den.e.z - num.e.z)};
+}
+// Below this the FP32 transmittance loses precision (subnormal range).
+constexpr float kTinyTransmittance = 1e-30f;
+ATMO_HD bool AnyTiny(F3 t) {
+  return t.x < kTinyTransmittance || t.y < kTinyTransmittance || t.z < kTinyTransmittance;
+}
+
+// rho^2 - rmu^2 from FP32 inputs, as a product of two factors.
+ATMO_HD float ImpactExcess(float rho, float rmu) { return (rho - rmu) * (rho + rmu); }
+
 ATMO_HD F3 TransmittanceToTop(const Consts& c, const Shape& s, const float4* T, float rho,
                               float r, float rmu) {
-  float2 uv = TransmittanceUv(c, s, rho, r, rmu);
-  return Bilinear(T, s.tw, s.th, uv.x, uv.y);
+  return TransmittanceLookup(c, s, T, rho, r, rmu, ImpactExcess(rho, rmu));
 }
 
 // GetTransmittance (functions.glsl:493-515) for the segment of length d from
-// (rho, r, rmu); t_start is TransmittanceToTop at the start point in the
-// direction the reference uses (-mu when the ray hits the ground).
-ATMO_HD F3 SegmentTransmittance(const Consts& c, const Shape& s, const float4* T, float rmu,
-                                const RadialPoint& pd, float d, bool ground, F3 t_start) {
+// (rho, r, rmu) with invariant impact excess delta; `start` is the lookup at
+// the start point in the direction the reference uses (-mu when the ray hits
+// the ground).  When that is tiny the ratio is formed from optical depths.
+// The start point's lookup, in both forms.
+struct TStart {
+  F3 t;        // linear
+  TExp x;      // m * exp(-e), only filled when tiny
+  bool tiny;   // t below kTinyTransmittance in some channel
+};
+ATMO_HD TStart MakeTStart(const Consts& c, const Shape& s, const float4* T, const float4* Tau,
+                          float rho, float r, float rmu, float delta) {
+  TCoords tc = TransmittanceCoords(c, s, rho, r, rmu, delta);
+  TStart st;
+  st.t = FetchTransmittance(T, tc);
+  st.tiny = AnyTiny(st.t);
+  st.x.m = f3(1.0f);
+  st.x.e = f3(0.0f);
+  if (st.tiny) st.x = FetchTau(Tau, tc);
+  return st;
+}
+
+ATMO_HD F3 SegmentTransmittance(const Consts& c, const Shape& s, const float4* T,
+                                const float4* Tau, float rmu, float delta,
+                                const RadialPoint& pd, float d, bool ground,
+                                const TStart& start) {
   float rmu_d = clampf(rmu + d, -pd.r, pd.r);
-  if (ground) {
-    return min3(TransmittanceToTop(c, s, T, pd.rho, pd.r, -rmu_d) / t_start, 1.0f);
+  TCoords tc = TransmittanceCoords(c, s, pd.rho, pd.r, ground ? -rmu_d : rmu_d, delta);
+  if (start.tiny) {
+    TExp x = FetchTau(Tau, tc);
+    return min3(ground ? TExpRatio(x, start.x) : TExpRatio(start.x, x), 1.0f);
   }
-  return min3(t_start / TransmittanceToTop(c, s, T, pd.rho, pd.r, rmu_d), 1.0f);
+  F3 t = FetchTransmittance(T, tc);
+  return min3(ground ? t / start.t : start.t / t, 1.0f);
 }
 
 // GetTransmittanceToSun (functions.glsl:552-563) at point p with r*mu_s = rmu_s.
@@ -349,9 +480,10 @@ struct TexelRow {        // one (r-slice k, mu-row j) of the scattering LUT
   float mu, rmu;         // mu and r*mu of the row
   float d;               // distance to the ray's boundary (ground or top)
   float omega_x;         // sqrt(1 - mu^2)
-  float q;               // ground: sqrt((r mu)^2 - rho^2); else rho^2 - (r mu)^2 (>= 0)
+  float q;               // ground: sqrt((r mu)^2 - rho^2); else 0
+  float delta;           // rho^2 - (r mu)^2, invariant along the ray
   int ground;            // ray_r_mu_intersects_ground
-  int pad[3];
+  int pad[2];
 };
 
 // rho^2 at distance t along the texel row's ray, where e = row.d - t is the
@@ -364,7 +496,7 @@ ATMO_HD float RayRho2(const TexelRow& row, float t, float e) {
   if (row.ground) return e * (e + 2.0f * row.q);
   if (row.rmu >= 0.0f) return fmaf(t, t + 2.0f * row.rmu, row.rho * row.rho);
   float u = t + row.rmu;
-  return fmaf(u, u, row.q);
+  return fmaf(u, u, row.delta);
 }
 struct TexelCol {        // one mu_s column c
   float mu_s, sin_s;     // mu_s, sqrt(1 - mu_s^2)
@@ -376,7 +508,8 @@ struct DensityRow {      // one (r-slice k, theta sample l) of the density integ
   float dist_ground;     // distance to the ground (0 when the ray misses it)
   int ground;            // RayIntersectsGround(r, cos theta_l)
   float u_mu;            // texture coordinate of (r, cos theta_l)
-  float pad0, pad1, pad2;
+  float delta;           // rho^2 - (r cos theta_l)^2, invariant along the row's ray
+  float pad1, pad2;
   float4 t_ground;       // transmittance to the ground x albedo / pi
 };
 

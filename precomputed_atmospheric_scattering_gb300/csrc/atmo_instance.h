@@ -15,6 +15,7 @@ struct Instance {
   Shape s;
   Tables tab;
   float4* T;        // transmittance, W_T x H_T
+  float4* Tau;      // optical depth -ln(T) of the same texels (internal)
   float4* I;        // irradiance accumulator, W_I x H_I
   float4* dI;       // delta irradiance
   float4* dR;       // delta Rayleigh; also delta multiple scattering (model.cc:897)

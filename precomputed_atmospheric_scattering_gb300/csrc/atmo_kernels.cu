@@ -27,7 +27,11 @@ k_transmittance(const Instance* __restrict__ insts, WorkList wl) {
     sums[1] += __shfl_xor_sync(0xffffffffu, sums[1], off, kTransmittanceLanes);
     sums[2] += __shfl_xor_sync(0xffffffffu, sums[2], off, kTransmittanceLanes);
   }
-  if (valid && lane == 0) in.T[texel] = TransmittanceFromLengths(in.c, ray, sums);
+  if (valid && lane == 0) {
+    F3 tau = OpticalDepth(in.c, ray, sums);
+    in.T[texel] = to4(exp3(f3(0.0f) - tau), 1.0f);
+    in.Tau[texel] = to4(tau, 0.0f);
+  }
 }
 
 // Direct irradiance texels, then the ground transmittance of every density

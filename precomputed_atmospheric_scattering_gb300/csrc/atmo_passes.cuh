@@ -150,11 +150,10 @@ ATMO_PASS void OpticalLengthPartial(const Consts& c, const TransmittanceRay& ray
   out[2] = ka.s;
 }
 
-ATMO_PASS float4 TransmittanceFromLengths(const Consts& c, const TransmittanceRay& ray,
-                                        const float sums[3]) {
-  F3 tau = c.rayleigh * (sums[0] * ray.dx) + c.mie_ext * (sums[1] * ray.dx) +
-           c.absorption * (sums[2] * ray.dx);
-  return to4(exp3(f3(0.0f) - tau), 1.0f);
+// Optical depth sum_i beta_i L_i of functions.glsl:306-320 (tau = -ln T).
+ATMO_PASS F3 OpticalDepth(const Consts& c, const TransmittanceRay& ray, const float sums[3]) {
+  return c.rayleigh * (sums[0] * ray.dx) + c.mie_ext * (sums[1] * ray.dx) +
+         c.absorption * (sums[2] * ray.dx);
 }
 
 // ---------------------------------------------------------------------------
@@ -183,9 +182,13 @@ ATMO_PASS float4 GroundRowTransmittance(const Instance& in, int e) {
   TexelRow row = in.tab.rows[k * s.smu];
   float rmu = row.r * dr.cos_t;
   float rmu_g = fminf(rmu + dr.dist_ground, 0.0f);
-  F3 t_start = TransmittanceToTop(c, s, in.T, row.rho, row.r, -rmu);
-  F3 t_end = TransmittanceToTop(c, s, in.T, 0.0f, c.Rb, -rmu_g);
-  F3 t = min3(t_end / t_start, 1.0f);
+  TStart start = MakeTStart(c, s, in.T, in.Tau, row.rho, row.r, -rmu, dr.delta);
+  RadialPoint ground_point;
+  ground_point.rho = 0.0f;
+  ground_point.r = c.Rb;
+  ground_point.h = 0.0f;
+  F3 t = SegmentTransmittance(c, s, in.T, in.Tau, rmu, dr.delta, ground_point,
+                              rmu_g - rmu, true, start);
   return to4(t * c.albedo * (1.0f / kPiF), 0.0f);
 }
 
@@ -203,13 +206,14 @@ ATMO_PASS void SingleScatteringTexel(const Instance& in, long long texel, F3* ra
   const bool ground = row.ground != 0;
   float dx = row.d / float(kSingleScatteringSamples);
   float rmu_s = row.r * ang.mu_s;
-  F3 t_start = TransmittanceToTop(c, s, in.T, row.rho, row.r, ground ? -row.rmu : row.rmu);
+  TStart start = MakeTStart(c, s, in.T, in.Tau, row.rho, row.r,
+                            ground ? -row.rmu : row.rmu, row.delta);
   F3 sum_r = f3(0.0f), sum_m = f3(0.0f);
   for (int i = 0; i <= kSingleScatteringSamples; ++i) {
     float d = float(i) * dx;
     float e = float(kSingleScatteringSamples - i) * dx;
     RadialPoint p = PointFromRho2(c, RayRho2(row, d, e));
-    F3 t = SegmentTransmittance(c, s, in.T, row.rmu, p, d, ground, t_start) *
+    F3 t = SegmentTransmittance(c, s, in.T, in.Tau, row.rmu, row.delta, p, d, ground, start) *
            TransmittanceToSun(c, s, in.T, p, fmaf(d, ang.nu, rmu_s));
     float w = (i == 0 || i == kSingleScatteringSamples) ? 0.5f : 1.0f;
     sum_r = fma3(t, ProfileDensity(c.prof_r, p.h) * w, sum_r);
@@ -345,7 +349,8 @@ ATMO_PASS F3 MultipleScatteringTexel(const Instance& in, long long texel, float*
   float dx = row.d / float(kMultipleScatteringSamples);
   float rmu_s = row.r * ang.mu_s;
   const float u_nu = (ang.nu + 1.0f) * 0.5f;
-  F3 t_start = TransmittanceToTop(c, s, in.T, row.rho, row.r, ground ? -row.rmu : row.rmu);
+  TStart start = MakeTStart(c, s, in.T, in.Tau, row.rho, row.r,
+                            ground ? -row.rmu : row.rmu, row.delta);
   F3 sum = f3(0.0f);
   for (int i = 0; i <= kMultipleScatteringSamples; ++i) {
     float d = float(i) * dx;
@@ -357,7 +362,7 @@ ATMO_PASS F3 MultipleScatteringTexel(const Instance& in, long long texel, float*
     float u_mu = UMuFromDistance(c, s, p, e, ground);
     Lookup4 L = MakeLookup(s, u_nu, UMuSFromMuS(c, s, mu_s_i), u_mu,
                            TexCoordFromUnitRange(p.rho / c.H, s.sr));
-    F3 t = SegmentTransmittance(c, s, in.T, row.rmu, p, d, ground, t_start);
+    F3 t = SegmentTransmittance(c, s, in.T, in.Tau, row.rmu, row.delta, p, d, ground, start);
     float w = (i == 0 || i == kMultipleScatteringSamples) ? 0.5f : 1.0f;
     sum = fma3(Scattering4(in.dJ, s, L) * t, dx * w, sum);
   }

@@ -44,6 +44,7 @@ atmo_status Storage::Allocate(const Shape& shape, bool combined_textures, bool h
 #define ATMO_ALLOC(ptr, bytes)                                   \
   if ((st = alloc(reinterpret_cast<void**>(&(ptr)), (bytes))) != ATMO_OK) return st;
   ATMO_ALLOC(T, nT * sizeof(float4));
+  ATMO_ALLOC(Tau, nT * sizeof(float4));
   ATMO_ALLOC(I, nI * sizeof(float4));
   ATMO_ALLOC(dI, nI * sizeof(float4));
   ATMO_ALLOC(dR, nS * sizeof(float4));
@@ -67,7 +68,7 @@ atmo_status Storage::Allocate(const Shape& shape, bool combined_textures, bool h
 void Storage::Free() {
   for (void* p : owned) cudaFree(p);
   owned.clear();
-  T = I = dI = dR = dM = dJ = S = M = nullptr;
+  T = Tau = I = dI = dR = dM = dJ = S = M = nullptr;
   S_half = M_half = nullptr;
   tab = Tables{};
 }
@@ -75,7 +76,7 @@ void Storage::Free() {
 size_t Storage::Bytes() const {
   const size_t nT = (size_t)s.t_texels(), nI = (size_t)s.i_texels(),
                nS = (size_t)s.s_texels();
-  size_t b = (nT + 2 * nI) * 16 + nS * 16 * (4 + (combined ? 0 : 1));
+  size_t b = (2 * nT + 2 * nI) * 16 + nS * 16 * (4 + (combined ? 0 : 1));
   if (half) b += nS * 8 * (combined ? 1 : 2);
   b += (size_t)s.sr * s.smu * sizeof(TexelRow) + s.smus * sizeof(TexelCol) +
        (size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow) + s.ih * sizeof(IrrRow) +

@@ -29,7 +29,7 @@ struct Storage {
   Shape s{};
   bool combined = true;
   bool half = false;
-  float4 *T = nullptr, *I = nullptr, *dI = nullptr, *dR = nullptr, *dM = nullptr,
+  float4 *T = nullptr, *Tau = nullptr, *I = nullptr, *dI = nullptr, *dR = nullptr, *dM = nullptr,
          *dJ = nullptr, *S = nullptr, *M = nullptr;
   void *S_half = nullptr, *M_half = nullptr;   // half-precision outputs
   Tables tab{};

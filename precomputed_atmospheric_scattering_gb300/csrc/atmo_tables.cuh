@@ -66,9 +66,10 @@ ATMO_HD TexelRow MakeTexelRow(const Consts& c, const Shape& s, int k, int j) {
   row.d = (float)(ground ? DistanceToBottom(Rb, r, mu) : DistanceToTop(Rt, r, mu));
   row.omega_x = (float)sqrt(fmax(1.0 - mu * mu, 0.0));
   double disc = rmu * rmu - rho * rho;   // r^2 (mu^2 - 1) + Rb^2
-  row.q = (float)(ground ? SafeSqrt(disc) : fmax(-disc, 0.0));
+  row.q = (float)(ground ? SafeSqrt(disc) : 0.0);
+  row.delta = (float)(-disc);
   row.ground = ground ? 1 : 0;
-  row.pad[0] = row.pad[1] = row.pad[2] = 0;
+  row.pad[0] = row.pad[1] = 0;
   return row;
 }
 
@@ -127,7 +128,8 @@ ATMO_HD DensityRow MakeDensityRow(const Consts& c, const Shape& s, int k, int l)
   d.ground = g ? 1 : 0;
   d.dist_ground = g ? (float)DistanceToBottom(Rb, r, ct) : 0.0f;
   d.u_mu = (float)UMu(c, s, r, ct, g);
-  d.pad0 = d.pad1 = d.pad2 = 0.0f;
+  d.delta = (float)(rho * rho - (r * ct) * (r * ct));
+  d.pad1 = d.pad2 = 0.0f;
   d.t_ground = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   return d;
 }

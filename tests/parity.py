@@ -31,3 +31,55 @@ def check(name, gpu, ref, tol, channels=3, report=None):
         report[name] = (mx, p99)
     assert mx <= tol, "%s: max relative error %.3g > %.3g (p99 %.3g)" % (name, mx, tol, p99)
     return mx
+
+
+# ---------------------------------------------------------------------------
+# Conditioning of the reference values (random planets).
+#
+# For very thick atmospheres the reference's FP64 result at some texels is
+# dominated by rounding: along rays that graze the ground, neighbouring
+# transmittance texels differ by many orders of magnitude, and the weight
+# that FP64 rounding puts on the brighter one decides the interpolated value.
+# Such a texel is detected by re-running the oracle with both radii scaled by
+# (1 + 1e-13): if its value moves by more than ROBUST_THRESHOLD relative, its
+# condition number exceeds ~1e8 and no FP32 (or differently ordered FP64)
+# evaluation reproduces it.  Random-planet tests compare only the other texels
+# and report how many were set aside; the Earth tests use no mask.
+# ---------------------------------------------------------------------------
+PERTURBATION = 1e-13
+ROBUST_THRESHOLD = 1e-5
+
+
+def robust_masks(O, atm, shape, orders, combined=True, base=None):
+    import ctypes as C
+    b = O.Atmosphere.from_buffer_copy(bytes(atm))
+    b.bottom_radius *= 1.0 + PERTURBATION
+    b.top_radius *= 1.0 + PERTURBATION
+    base = base or O.precompute(atm, shape, orders, combined=combined)
+    pert = O.precompute(b, shape, orders, combined=combined)
+    masks = {}
+    for k in ("transmittance", "scattering", "single_mie", "irradiance"):
+        ch = 4 if (k == "scattering" and combined) else 3
+        x = np.asarray(getattr(base, k))[..., :ch].reshape(-1, ch)
+        y = np.asarray(getattr(pert, k))[..., :ch].reshape(-1, ch)
+        scale = np.abs(x).max(axis=0)
+        scale = np.where(scale > 0, scale, 1.0)
+        den = np.maximum(np.abs(x), FLOOR * scale)
+        masks[k] = (np.abs(x - y) / den).max(axis=1) <= ROBUST_THRESHOLD
+    return base, masks
+
+
+def check_masked(name, gpu, ref, tol, mask, channels=3, report=None):
+    g = np.asarray(gpu)[..., :channels].reshape(-1, channels)[mask]
+    r = np.asarray(ref)[..., :channels].reshape(-1, channels)
+    scale = np.abs(r).max(axis=0)
+    scale = np.where(scale > 0, scale, 1.0)
+    r = r[mask]
+    den = np.maximum(np.abs(r), FLOOR * scale)
+    e = np.abs(g.astype(np.float64) - r) / den
+    mx = float(e.max()) if e.size else 0.0
+    if report is not None:
+        report[name] = (mx, int((~mask).sum()))
+    assert mx <= tol, "%s: max relative error %.3g > %.3g on %d robust texels (%d set aside)" % (
+        name, mx, tol, int(mask.sum()), int((~mask).sum()))
+    return mx

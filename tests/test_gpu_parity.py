@@ -10,7 +10,8 @@ import os
 import numpy as np
 import pytest
 
-from parity import (TOL_IRRADIANCE, TOL_SCATTERING, TOL_TRANSMITTANCE, check)
+from parity import (TOL_IRRADIANCE, TOL_SCATTERING, TOL_TRANSMITTANCE, check, check_masked,
+                    robust_masks)
 from test_capi_host import earth_model
 
 pytestmark = pytest.mark.gpu
@@ -63,16 +64,30 @@ def test_small_shape_earth_vs_oracle(atmo, oracle, torch, path, combined):
     compare(ref, gpu, combined)
 
 
+def compare_robust(oracle, atm, shape, orders, gpu, combined, report=None):
+    ref, masks = robust_masks(oracle, atm, shape, orders, combined)
+    T, S, M, I = gpu
+    check_masked("transmittance", T, ref.transmittance, TOL_TRANSMITTANCE,
+                 masks["transmittance"], report=report)
+    check_masked("scattering", S, ref.scattering, TOL_SCATTERING, masks["scattering"],
+                 channels=4 if combined else 3, report=report)
+    if not combined:
+        check_masked("single_mie", M, ref.single_mie, TOL_SCATTERING, masks["single_mie"],
+                     report=report)
+    check_masked("irradiance", I, ref.irradiance, TOL_IRRADIANCE, masks["irradiance"],
+                 report=report)
+
+
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
 def test_medium_shape_random_atmospheres_vs_oracle(atmo, oracle, torch, path):
-    """Non-Earth planets: seeded draws over the batched-rebuild ranges."""
+    """Non-Earth planets: seeded draws over the batched-rebuild ranges, compared
+    on the texels where the FP64 reference is not rounding-dominated."""
     rng = np.random.default_rng(1234)
     for trial in range(2):
         atm = random_atmosphere(oracle, rng)
         orders = int(rng.integers(2, 5))
-        ref = oracle.precompute(atm, oracle.MEDIUM_SHAPE, orders, combined=False)
         gpu = gpu_precompute(atmo, torch, atm, oracle.MEDIUM_SHAPE, orders, False, path)
-        compare(ref, gpu, False)
+        compare_robust(oracle, atm, oracle.MEDIUM_SHAPE, orders, gpu, False)
 
 
 def random_atmosphere(O, rng):
