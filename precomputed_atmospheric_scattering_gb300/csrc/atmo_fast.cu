@@ -1,5 +1,18 @@
-// atmo_fast.cu -- fast-path kernels (slab-restructured scattering density and
-// multiple scattering) and the FP16 output conversion.
+// atmo_fast.cu -- fast-path kernels: the slab-restructured scattering density
+// (the dominant pass, functions.glsl:1163-1260) and the FP16 output conversion.
+//
+// Scattering density, restructured.  For a texel at r-slice k and mu_s column
+// c, every incoming-radiance lookup of ComputeScatteringDensity is made at the
+// texel's own r and mu_s, whose texture coordinates land on the centres of
+// slice k and column c (the texel mapping and the lookup mapping are inverse
+// to each other), while mu = cos(theta_l) takes one of 16 values shared by
+// all texels of the slice and only nu varies with the direction.  A block
+// therefore owns the slab (k, c) -- the NU x MU texels with that r and mu_s --
+// and stages in shared memory, per theta row l and nu node n, the previous
+// order's radiance bilinearly interpolated in mu: L[l][n].  The quadrilinear
+// lookup of a direction reduces to a lerp between L[l][n0] and L[l][n0 + 1].
+// The ground term reads the bottom row of the irradiance LUT (the ground
+// point is at r = Rb, on row 0's centre), also staged in shared memory.
 #include <cuda_fp16.h>
 
 #include "atmo_kernels.h"
@@ -7,13 +20,134 @@
 
 namespace atmo {
 
-int DensityFastTiles(const Shape& s) {
-  return (int)((s.s_texels() + kTexelThreads - 1) / kTexelThreads);
+constexpr int kDensityFastThreads = 256;
+
+int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
+
+// Shared memory of one block, bytes.
+int DensityFastSmem(const Shape& s, int order) {
+  return ((order == 2 ? 2 : 1) * kDensityThetaSamples * s.snu + s.iw) * (int)sizeof(float4);
 }
+
+template <bool kOrder2>
+__global__ void __launch_bounds__(kDensityFastThreads)
+k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
+  extern __shared__ float4 smem[];
+  int local;
+  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
+  const Shape s = in.s;
+  const Consts& c = in.c;
+  const int NU = s.snu, W = s.sw();
+  const int k = local / s.smus, col = local % s.smus;
+  float4* LR = smem;                                   // [16][NU] Rayleigh / multiple
+  float4* LM = smem + kDensityThetaSamples * NU;       // [16][NU] Mie (order 2)
+  float4* IR = smem + (kOrder2 ? 2 : 1) * kDensityThetaSamples * NU;   // [iw]
+  const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
+
+  // Stage the previous order, bilinear in mu, at column (n * MU_S + col) of slice k.
+  for (int e = threadIdx.x; e < kDensityThetaSamples * NU; e += blockDim.x) {
+    const int l = e / NU, n = e % NU;
+    const float Y = drows[l].u_mu * float(s.smu) - 0.5f;
+    const float fy = floorf(Y);
+    const float wy = Y - fy;
+    const int y0 = ClampIdx((int)fy, s.smu), y1 = ClampIdx((int)fy + 1, s.smu);
+    const long long base = (long long)k * s.smu * W + n * s.smus + col;
+    const float4 a = __ldg(in.dR + base + (long long)y0 * W);
+    const float4 b = __ldg(in.dR + base + (long long)y1 * W);
+    LR[e] = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
+                        fmaf(wy, b.z - a.z, a.z), 0.0f);
+    if (kOrder2) {
+      const float4 p = __ldg(in.dM + base + (long long)y0 * W);
+      const float4 q = __ldg(in.dM + base + (long long)y1 * W);
+      LM[e] = make_float4(fmaf(wy, q.x - p.x, p.x), fmaf(wy, q.y - p.y, p.y),
+                          fmaf(wy, q.z - p.z, p.z), 0.0f);
+    }
+  }
+  for (int e = threadIdx.x; e < s.iw; e += blockDim.x) IR[e] = __ldg(in.dI + e);
+  __syncthreads();
+
+  const TexelCol cc = in.tab.cols[col];
+  const float half_nu = 0.5f * float(NU - 1);
+  const float iw1 = float(s.iw - 1);
+  const float inv_rb = 1.0f / c.Rb;
+  const float dtdp = (kPiF / 16.0f) * (kPiF / 16.0f);
+  const int texels = NU * s.smu;
+  for (int t = threadIdx.x; t < texels; t += blockDim.x) {
+    const int j = t % s.smu, n = t / s.smu;
+    const TexelRow row = in.tab.rows[k * s.smu + j];
+    const TexelAngles ang = MakeAngles(s, row, cc, n);
+    const float rmu_s = row.r * ang.mu_s;
+    F3 sum_r = f3(0.0f), sum_m = f3(0.0f);   // sums of L * P_R(nu2) / c.ray_k and L * P_M(nu2)
+    for (int l = 0; l < kDensityThetaSamples; ++l) {
+      const DensityRow dr = drows[l];
+      const float A = ang.mu_s * dr.cos_t, B = ang.mu * dr.cos_t;
+      const float4* Lr = LR + l * NU;
+      const float4* Lm = LM + l * NU;
+      const F3 tg = f3(dr.t_ground);
+      F3 row_r = f3(0.0f), row_m = f3(0.0f);
+#pragma unroll 4
+      for (int m = 0; m < kDensityPhiSamples; ++m) {
+        const float2 cs = c_density_phi[m];
+        const float a = fmaf(ang.sx, cs.x, ang.sy * cs.y);
+        const float nu1 = fmaf(dr.sin_t, a, A);
+        const float nu2 = fmaf(dr.sin_t, ang.omega_x * cs.x, B);
+        // nu lerp between staged nodes (functions.glsl:967-975).
+        const float u = clampf(fmaf(nu1, half_nu, half_nu), 0.0f, float(NU - 1));
+        const int n0 = min((int)u, NU - 2);
+        const float w = u - float(n0);
+        float4 p0 = Lr[n0], p1 = Lr[n0 + 1];
+        F3 L = F3{fmaf(w, p1.x - p0.x, p0.x), fmaf(w, p1.y - p0.y, p0.y),
+                  fmaf(w, p1.z - p0.z, p0.z)};
+        if (kOrder2) {
+          // Single scattering with its phase functions at nu1 (:998-1004).
+          const float4 q0 = Lm[n0], q1 = Lm[n0 + 1];
+          const F3 M = F3{fmaf(w, q1.x - q0.x, q0.x), fmaf(w, q1.y - q0.y, q0.y),
+                          fmaf(w, q1.z - q0.z, q0.z)};
+          L = L * RayleighPhase(c, nu1) + M * MiePhase(c, nu1);
+        }
+        if (dr.ground) {
+          // Ground bounce: the ground point is at radius Rb, so the cosine of
+          // its normal with the sun is (r mu_s + dist nu1) / Rb; the irradiance
+          // lookup at r = Rb reads row 0 of the LUT.
+          const float mu_g = fmaf(dr.dist_ground, nu1, rmu_s) * inv_rb;
+          const float X = clampf(fmaf(mu_g, 0.5f, 0.5f), 0.0f, 1.0f) * iw1;
+          const int i0 = min((int)X, s.iw - 2);
+          const float wi = X - float(i0);
+          const float4 e0 = IR[i0], e1 = IR[i0 + 1];
+          L = fma3(tg, F3{fmaf(wi, e1.x - e0.x, e0.x), fmaf(wi, e1.y - e0.y, e0.y),
+                          fmaf(wi, e1.z - e0.z, e0.z)}, L);
+        }
+        // Phase functions at nu2 (functions.glsl:739-747, :1245-1254).
+        const float q = fmaf(nu2, nu2, 1.0f);
+        const float tm = fmaf(c.m2g, nu2, c.g2p1);
+        const float rs = rsqrtf(tm);
+        row_r = fma3(L, q, row_r);
+        row_m = fma3(L, q * (rs * rs * rs), row_m);
+      }
+      const float dw = dtdp * dr.sin_t;
+      sum_r = fma3(row_r, dw, sum_r);
+      sum_m = fma3(row_m, dw, sum_m);
+    }
+    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
+    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+    const F3 J = a_r * sum_r + a_m * sum_m;
+    const long long texel = ((long long)k * s.smu + j) * W + n * s.smus + col;
+    in.dJ[texel] = to4(J, 1.0f);
+  }
+}
+
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
-                              cudaStream_t st) {
-  return LaunchDensityPlain(insts, wl, tiles, order, st);
+                              int smem_bytes, cudaStream_t st) {
+  // smem_bytes: the largest DensityFastSmem of the work list's instances.
+  const size_t bytes = (size_t)smem_bytes;
+  if (order == 2) {
+    k_density_fast<true><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl);
+  } else {
+    k_density_fast<false><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl);
+  }
+  return cudaGetLastError();
 }
+
 cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, cudaStream_t st) {
   return LaunchMultiplePlain(insts, wl, tiles, st);
 }

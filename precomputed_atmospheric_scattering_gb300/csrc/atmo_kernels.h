@@ -23,8 +23,9 @@ cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
                                 cudaStream_t st);
 // Fast path (atmo_fast.cu).
 int DensityFastTiles(const Shape& s);
+int DensityFastSmem(const Shape& s, int order);
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
-                              cudaStream_t st);
+                              int smem_bytes, cudaStream_t st);
 cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles,
                                cudaStream_t st);
 // Final conversion of the scattering accumulators to half precision.

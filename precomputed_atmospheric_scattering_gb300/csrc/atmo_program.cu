@@ -112,9 +112,11 @@ Program::~Program() {
   if (d_blob_) cudaFree(d_blob_);
 }
 
-int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles) {
+int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles,
+                         int* smem) {
   std::vector<int> inst, start;
   int t = 0;
+  if (smem) *smem = 0;
   for (int m : members) {
     if ((pass == Pass::kDensity || pass == Pass::kMultiple) && orders[m] < (unsigned)order)
       continue;
@@ -122,6 +124,10 @@ int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, 
     inst.push_back(m);
     start.push_back(t);
     t += Tiles(pass, slots[m].s, path);
+    if (smem && pass == Pass::kDensity && path == ATMO_PATH_FAST) {
+      int b = DensityFastSmem(slots[m].s, order);
+      *smem = b > *smem ? b : *smem;
+    }
   }
   *tiles = t;
   if (inst.empty()) return -1;
@@ -135,9 +141,9 @@ int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, 
 
 void Program::AddStage(const std::vector<int>& members, bool transmittance_only) {
   auto add = [&](Pass p, int order) {
-    int tiles = 0;
-    int wl = AddWorkList(members, p, order, &tiles);
-    if (wl >= 0 && tiles > 0) steps_.push_back(Step{p, order, wl, tiles});
+    int tiles = 0, smem = 0;
+    int wl = AddWorkList(members, p, order, &tiles, &smem);
+    if (wl >= 0 && tiles > 0) steps_.push_back(Step{p, order, wl, tiles, smem});
   };
   if (transmittance_only) {
     add(Pass::kTransmittance, 0);
@@ -160,7 +166,7 @@ void Program::AddToHalf(const std::vector<int>& members) {
   for (int m : members) {
     int tiles = 0;
     int wl = AddWorkList({m}, Pass::kToHalf, 0, &tiles);
-    if (wl >= 0) steps_.push_back(Step{Pass::kToHalf, 0, wl, tiles});
+    if (wl >= 0) steps_.push_back(Step{Pass::kToHalf, 0, wl, tiles, 0});
   }
 }
 
@@ -239,8 +245,9 @@ atmo_status Program::LaunchStep(size_t i, cudaStream_t st) {
       case Pass::kDirect: e = LaunchDirectIrradiance(d_slots_, wl, step.tiles, st); break;
       case Pass::kSingle: e = LaunchSingleScattering(d_slots_, wl, step.tiles, st); break;
       case Pass::kDensity:
-        e = path == ATMO_PATH_FAST ? LaunchDensityFast(d_slots_, wl, step.tiles, step.order, st)
-                                   : LaunchDensityPlain(d_slots_, wl, step.tiles, step.order, st);
+        e = path == ATMO_PATH_FAST
+                ? LaunchDensityFast(d_slots_, wl, step.tiles, step.order, step.smem, st)
+                : LaunchDensityPlain(d_slots_, wl, step.tiles, step.order, st);
         break;
       case Pass::kIndirect:
         e = LaunchIndirectIrradiance(d_slots_, wl, step.tiles, step.order, st);

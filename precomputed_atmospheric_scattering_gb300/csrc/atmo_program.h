@@ -47,6 +47,7 @@ struct Step {
   int order;      // scattering order of density / multiple; order-1 for indirect
   int wl;         // work-list index
   int tiles;      // blocks of the launch
+  int smem;       // dynamic shared memory bytes (fast density)
 };
 
 // A program: a sequence of stages; a stage runs the full precomputation of a
@@ -75,7 +76,8 @@ class Program {
   std::vector<Step> const& steps() const { return steps_; }
 
  private:
-  int AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles);
+  int AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles,
+                  int* smem = nullptr);
   std::vector<Step> steps_;
   std::vector<int> blob_;              // inst[] then start[] of every work list
   std::vector<std::pair<int, int>> wl_offsets_;  // (offset, count)
