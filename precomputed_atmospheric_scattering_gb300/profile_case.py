@@ -6,7 +6,7 @@ B Earth atmospheres of one LUT shape, `runs` times.
 import argparse
 import math
 
-from . import Atmosphere, Batch, PATH_FAST, PATH_PLAIN, lib, synchronize_stream
+from . import Atmosphere, Batch, lib, synchronize_stream
 
 SHAPES = {"default": (256, 64, 32, 128, 32, 8, 64, 16),
           "medium": (128, 32, 8, 32, 16, 8, 32, 8),
@@ -47,11 +47,11 @@ def main():
     p.add_argument("--shape", default="default", choices=sorted(SHAPES))
     p.add_argument("--orders", type=int, default=4)
     p.add_argument("--runs", type=int, default=1)
-    p.add_argument("--plain", action="store_true")
+    p.add_argument("--no-graph", action="store_true", help="launch the passes directly")
     a = p.parse_args()
     lib()
     b = Batch([earth()] * a.batch, [SHAPES[a.shape]] * a.batch, a.orders)
-    if a.plain:
+    if a.no_graph:
         for _ in range(a.runs):
             b.time_passes()
     else:
