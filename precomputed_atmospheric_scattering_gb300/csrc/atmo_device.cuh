@@ -414,38 +414,49 @@ ATMO_HD Lookup4 MakeLookup(const Shape& s, float u_nu, float u_mu_s, float u_mu,
 
 ATMO_HD int ClampIdx(int i, int n) { return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); }
 
-ATMO_HD F3 Trilinear(const float4* __restrict__ tex, const Shape& s, float x, float y,
-                     float z) {
+// The 4D lookup of functions.glsl:958-976: two trilinear fetches (the nu
+// nodes at x0 and x1) that share their y (mu) and z (r) interpolation, with
+// the nu lerp folded into the x weights.  32-bit indices (the scattering LUT
+// has fewer than 2^31 texels).
+ATMO_HD F3 Scattering4(const float4* __restrict__ tex, const Shape& s, const Lookup4& L) {
   const int W = s.sw(), Hh = s.smu, D = s.sr;
-  float fx = floorf(x), fy = floorf(y), fz = floorf(z);
-  float a = x - fx, b = y - fy, cc = z - fz;
-  int i0 = ClampIdx((int)fx, W), i1 = ClampIdx((int)fx + 1, W);
-  int j0 = ClampIdx((int)fy, Hh), j1 = ClampIdx((int)fy + 1, Hh);
-  int k0 = ClampIdx((int)fz, D), k1 = ClampIdx((int)fz + 1, D);
+  const float fy = floorf(L.y), fz = floorf(L.z);
+  const float b = L.y - fy, c = L.z - fz;
+  const int j0 = ClampIdx((int)fy, Hh), j1 = ClampIdx((int)fy + 1, Hh);
+  const int k0 = ClampIdx((int)fz, D), k1 = ClampIdx((int)fz + 1, D);
+  const int r00 = (k0 * Hh + j0) * W, r01 = (k0 * Hh + j1) * W;
+  const int r10 = (k1 * Hh + j0) * W, r11 = (k1 * Hh + j1) * W;
+  const float w00 = (1.0f - b) * (1.0f - c), w01 = b * (1.0f - c);
+  const float w10 = (1.0f - b) * c, w11 = b * c;
   F3 acc = f3(0.0f);
-  const int ii[2] = {i0, i1}, jj[2] = {j0, j1}, kk[2] = {k0, k1};
-  const float wi[2] = {1.0f - a, a}, wj[2] = {1.0f - b, b}, wk[2] = {1.0f - cc, cc};
 #pragma unroll
-  for (int dk = 0; dk < 2; ++dk)
-#pragma unroll
-    for (int dj = 0; dj < 2; ++dj)
-#pragma unroll
-      for (int di = 0; di < 2; ++di) {
-        long long idx = ((long long)kk[dk] * Hh + jj[dj]) * W + ii[di];
+  for (int node = 0; node < 2; ++node) {
+    const float x = node == 0 ? L.x0 : L.x1;
+    const float wn = node == 0 ? 1.0f - L.lerp_nu : L.lerp_nu;
+    const float fx = floorf(x);
+    const float a = x - fx;
+    const int i0 = ClampIdx((int)fx, W), i1 = ClampIdx((int)fx + 1, W);
+    const float wa0 = (1.0f - a) * wn, wa1 = a * wn;
 #ifdef __CUDA_ARCH__
-        float4 t = __ldg(tex + idx);
+#define ATMO_TAP(idx) __ldg(tex + (idx))
 #else
-        float4 t = tex[idx];
+#define ATMO_TAP(idx) tex[(idx)]
 #endif
-        acc = fma3(f3(t), wi[di] * wj[dj] * wk[dk], acc);
-      }
+    const float4 t0 = ATMO_TAP(r00 + i0), t1 = ATMO_TAP(r00 + i1);
+    const float4 t2 = ATMO_TAP(r01 + i0), t3 = ATMO_TAP(r01 + i1);
+    const float4 t4 = ATMO_TAP(r10 + i0), t5 = ATMO_TAP(r10 + i1);
+    const float4 t6 = ATMO_TAP(r11 + i0), t7 = ATMO_TAP(r11 + i1);
+#undef ATMO_TAP
+    const float v0 = wa0 * w00, v1 = wa1 * w00, v2 = wa0 * w01, v3 = wa1 * w01;
+    const float v4 = wa0 * w10, v5 = wa1 * w10, v6 = wa0 * w11, v7 = wa1 * w11;
+    acc.x += t0.x * v0 + t1.x * v1 + t2.x * v2 + t3.x * v3 + t4.x * v4 + t5.x * v5 +
+             t6.x * v6 + t7.x * v7;
+    acc.y += t0.y * v0 + t1.y * v1 + t2.y * v2 + t3.y * v3 + t4.y * v4 + t5.y * v5 +
+             t6.y * v6 + t7.y * v7;
+    acc.z += t0.z * v0 + t1.z * v1 + t2.z * v2 + t3.z * v3 + t4.z * v4 + t5.z * v5 +
+             t6.z * v6 + t7.z * v7;
+  }
   return acc;
-}
-
-ATMO_HD F3 Scattering4(const float4* tex, const Shape& s, const Lookup4& L) {
-  F3 a = Trilinear(tex, s, L.x0, L.y, L.z);
-  F3 b = Trilinear(tex, s, L.x1, L.y, L.z);
-  return a * (1.0f - L.lerp_nu) + b * L.lerp_nu;
 }
 
 // functions.glsl:739-747

@@ -24,9 +24,26 @@ constexpr int kDensityFastThreads = 256;
 
 int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
 
-// Shared memory of one block, bytes.
+// Shared memory of one block, bytes: per staged species a [16][NU] float4
+// table (L.x, L.y, L.z, D.x) and a [16][NU] float2 table (D.y, D.z), where
+// D = L[n + 1] - L[n] is the slope towards the next nu node; then the bottom
+// row of the irradiance LUT; then a float temporary per table entry.
 int DensityFastSmem(const Shape& s, int order) {
-  return ((order == 2 ? 2 : 1) * kDensityThetaSamples * s.snu + s.iw) * (int)sizeof(float4);
+  const int species = order == 2 ? 2 : 1;
+  return species * kDensityThetaSamples * s.snu *
+             (int)(sizeof(float4) + sizeof(float2) + sizeof(float)) +
+         s.iw * (int)sizeof(float4);
+}
+
+// The staged radiance at nu1 of theta row l: L[n0] + w D[n0].
+__device__ __forceinline__ F3 NuLerp(const float4* __restrict__ P, const float2* __restrict__ Q,
+                                     float nu1, float half_nu, float top, int nmax) {
+  const float u = clampf(fmaf(nu1, half_nu, half_nu), 0.0f, top);
+  const int n0 = min((int)u, nmax);
+  const float w = u - float(n0);
+  const float4 p = P[n0];
+  const float2 q = Q[n0];
+  return F3{fmaf(w, p.w, p.x), fmaf(w, q.x, p.y), fmaf(w, q.y, p.z)};
 }
 
 template <bool kOrder2>
@@ -36,39 +53,67 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   int local;
   const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
   const Shape s = in.s;
-  const Consts& c = in.c;
   const int NU = s.snu, W = s.sw();
   const int k = local / s.smus, col = local % s.smus;
-  float4* LR = smem;                                   // [16][NU] Rayleigh / multiple
-  float4* LM = smem + kDensityThetaSamples * NU;       // [16][NU] Mie (order 2)
-  float4* IR = smem + (kOrder2 ? 2 : 1) * kDensityThetaSamples * NU;   // [iw]
+  const int rows_nu = kDensityThetaSamples * NU;
+  float4* PR = smem;                                          // Rayleigh / multiple
+  float2* QR = reinterpret_cast<float2*>(PR + rows_nu);
+  float4* PM = reinterpret_cast<float4*>(QR + rows_nu);        // Mie (order 2)
+  float2* QM = reinterpret_cast<float2*>(PM + rows_nu);
+  float4* IR = kOrder2 ? reinterpret_cast<float4*>(QM + rows_nu) : PM;   // [iw]
   const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
 
-  // Stage the previous order, bilinear in mu, at column (n * MU_S + col) of slice k.
-  for (int e = threadIdx.x; e < kDensityThetaSamples * NU; e += blockDim.x) {
+  // Stage the previous order, bilinear in mu, at column (n * MU_S + col) of
+  // slice k: first the values, then (after a barrier) the slopes.
+  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
     const int l = e / NU, n = e % NU;
     const float Y = drows[l].u_mu * float(s.smu) - 0.5f;
     const float fy = floorf(Y);
     const float wy = Y - fy;
     const int y0 = ClampIdx((int)fy, s.smu), y1 = ClampIdx((int)fy + 1, s.smu);
-    const long long base = (long long)k * s.smu * W + n * s.smus + col;
-    const float4 a = __ldg(in.dR + base + (long long)y0 * W);
-    const float4 b = __ldg(in.dR + base + (long long)y1 * W);
-    LR[e] = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
+    const int base = k * s.smu * W + n * s.smus + col;
+    const float4 a = __ldg(in.dR + base + y0 * W);
+    const float4 b = __ldg(in.dR + base + y1 * W);
+    PR[e] = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
                         fmaf(wy, b.z - a.z, a.z), 0.0f);
     if (kOrder2) {
-      const float4 p = __ldg(in.dM + base + (long long)y0 * W);
-      const float4 q = __ldg(in.dM + base + (long long)y1 * W);
-      LM[e] = make_float4(fmaf(wy, q.x - p.x, p.x), fmaf(wy, q.y - p.y, p.y),
+      const float4 p = __ldg(in.dM + base + y0 * W);
+      const float4 q = __ldg(in.dM + base + y1 * W);
+      PM[e] = make_float4(fmaf(wy, q.x - p.x, p.x), fmaf(wy, q.y - p.y, p.y),
                           fmaf(wy, q.z - p.z, p.z), 0.0f);
     }
   }
   for (int e = threadIdx.x; e < s.iw; e += blockDim.x) IR[e] = __ldg(in.dI + e);
   __syncthreads();
+  // Slopes towards the next node (0 at the last node): y, z into Q, x into a
+  // temporary, then x into P.w once every value has been read.
+  float* TX = reinterpret_cast<float*>(IR + s.iw);                 // [species][rows_nu]
+  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
+    const bool last = (e % NU) == NU - 1;
+    const float4 v = PR[e], nx = last ? v : PR[e + 1];
+    QR[e] = make_float2(nx.y - v.y, nx.z - v.z);
+    TX[e] = nx.x - v.x;
+    if (kOrder2) {
+      const float4 vm = PM[e], nm = last ? vm : PM[e + 1];
+      QM[e] = make_float2(nm.y - vm.y, nm.z - vm.z);
+      TX[rows_nu + e] = nm.x - vm.x;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
+    PR[e].w = TX[e];
+    if (kOrder2) PM[e].w = TX[rows_nu + e];
+  }
+  __syncthreads();
 
+  const Consts& c = in.c;
+  const float m2g = c.m2g, g2p1 = c.g2p1, ray_k = c.ray_k, mie_k = c.mie_k;
   const TexelCol cc = in.tab.cols[col];
   const float half_nu = 0.5f * float(NU - 1);
+  const float top = float(NU - 1);
+  const int nmax = NU - 2;
   const float iw1 = float(s.iw - 1);
+  const int imax = s.iw - 2;
   const float inv_rb = 1.0f / c.Rb;
   const float dtdp = (kPiF / 16.0f) * (kPiF / 16.0f);
   const int texels = NU * s.smu;
@@ -77,61 +122,67 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     const TexelRow row = in.tab.rows[k * s.smu + j];
     const TexelAngles ang = MakeAngles(s, row, cc, n);
     const float rmu_s = row.r * ang.mu_s;
-    F3 sum_r = f3(0.0f), sum_m = f3(0.0f);   // sums of L * P_R(nu2) / c.ray_k and L * P_M(nu2)
+    F3 sum_r = f3(0.0f), sum_m = f3(0.0f);   // sums of L (1 + nu2^2) and L P_M(nu2) / mie_k
     for (int l = 0; l < kDensityThetaSamples; ++l) {
       const DensityRow dr = drows[l];
       const float A = ang.mu_s * dr.cos_t, B = ang.mu * dr.cos_t;
-      const float4* Lr = LR + l * NU;
-      const float4* Lm = LM + l * NU;
+      const float sxs = ang.sx * dr.sin_t, sys = ang.sy * dr.sin_t;
+      const float oxs = ang.omega_x * dr.sin_t;
+      const float4* Pr = PR + l * NU;
+      const float2* Qr = QR + l * NU;
+      const float4* Pm = PM + l * NU;
+      const float2* Qm = QM + l * NU;
       const F3 tg = f3(dr.t_ground);
+      const bool ground = dr.ground != 0;
       F3 row_r = f3(0.0f), row_m = f3(0.0f);
-#pragma unroll 4
-      for (int m = 0; m < kDensityPhiSamples; ++m) {
+      // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions
+      // of the outgoing direction; nu1 differs by the sign of sy sin(phi).
+#pragma unroll 2
+      for (int m = 0; m < kDensityPhiSamples / 2; ++m) {
         const float2 cs = c_density_phi[m];
-        const float a = fmaf(ang.sx, cs.x, ang.sy * cs.y);
-        const float nu1 = fmaf(dr.sin_t, a, A);
-        const float nu2 = fmaf(dr.sin_t, ang.omega_x * cs.x, B);
-        // nu lerp between staged nodes (functions.glsl:967-975).
-        const float u = clampf(fmaf(nu1, half_nu, half_nu), 0.0f, float(NU - 1));
-        const int n0 = min((int)u, NU - 2);
-        const float w = u - float(n0);
-        float4 p0 = Lr[n0], p1 = Lr[n0 + 1];
-        F3 L = F3{fmaf(w, p1.x - p0.x, p0.x), fmaf(w, p1.y - p0.y, p0.y),
-                  fmaf(w, p1.z - p0.z, p0.z)};
-        if (kOrder2) {
-          // Single scattering with its phase functions at nu1 (:998-1004).
-          const float4 q0 = Lm[n0], q1 = Lm[n0 + 1];
-          const F3 M = F3{fmaf(w, q1.x - q0.x, q0.x), fmaf(w, q1.y - q0.y, q0.y),
-                          fmaf(w, q1.z - q0.z, q0.z)};
-          L = L * RayleighPhase(c, nu1) + M * MiePhase(c, nu1);
-        }
-        if (dr.ground) {
-          // Ground bounce: the ground point is at radius Rb, so the cosine of
-          // its normal with the sun is (r mu_s + dist nu1) / Rb; the irradiance
-          // lookup at r = Rb reads row 0 of the LUT.
-          const float mu_g = fmaf(dr.dist_ground, nu1, rmu_s) * inv_rb;
-          const float X = clampf(fmaf(mu_g, 0.5f, 0.5f), 0.0f, 1.0f) * iw1;
-          const int i0 = min((int)X, s.iw - 2);
-          const float wi = X - float(i0);
-          const float4 e0 = IR[i0], e1 = IR[i0 + 1];
-          L = fma3(tg, F3{fmaf(wi, e1.x - e0.x, e0.x), fmaf(wi, e1.y - e0.y, e0.y),
-                          fmaf(wi, e1.z - e0.z, e0.z)}, L);
+        const float base = fmaf(sxs, cs.x, A);
+        const float dl = sys * cs.y;
+        const float nu2 = fmaf(oxs, cs.x, B);
+        F3 Ls = f3(0.0f);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          const float nu1 = side == 0 ? base + dl : base - dl;
+          F3 L = NuLerp(Pr, Qr, nu1, half_nu, top, nmax);
+          if (kOrder2) {
+            // Single scattering with its phase functions at nu1 (:998-1004).
+            const F3 M = NuLerp(Pm, Qm, nu1, half_nu, top, nmax);
+            const float q1 = fmaf(nu1, nu1, 1.0f);
+            const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
+            L = L * (ray_k * q1) + M * (mie_k * q1 * (r1 * r1 * r1));
+          }
+          if (ground) {
+            // Ground bounce: the ground point is at radius Rb, so the cosine
+            // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
+            // irradiance lookup at r = Rb reads row 0 of the LUT.
+            const float mu_g = fmaf(dr.dist_ground, nu1, rmu_s) * inv_rb;
+            const float X = clampf(fmaf(mu_g, 0.5f, 0.5f), 0.0f, 1.0f) * iw1;
+            const int i0 = min((int)X, imax);
+            const float wi = X - float(i0);
+            const float4 e0 = IR[i0], e1 = IR[i0 + 1];
+            L = fma3(tg, F3{fmaf(wi, e1.x - e0.x, e0.x), fmaf(wi, e1.y - e0.y, e0.y),
+                            fmaf(wi, e1.z - e0.z, e0.z)}, L);
+          }
+          Ls += L;
         }
         // Phase functions at nu2 (functions.glsl:739-747, :1245-1254).
         const float q = fmaf(nu2, nu2, 1.0f);
-        const float tm = fmaf(c.m2g, nu2, c.g2p1);
-        const float rs = rsqrtf(tm);
-        row_r = fma3(L, q, row_r);
-        row_m = fma3(L, q * (rs * rs * rs), row_m);
+        const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
+        row_r = fma3(Ls, q, row_r);
+        row_m = fma3(Ls, q * (rs * rs * rs), row_m);
       }
       const float dw = dtdp * dr.sin_t;
       sum_r = fma3(row_r, dw, sum_r);
       sum_m = fma3(row_m, dw, sum_m);
     }
-    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
-    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * ray_k);
+    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * mie_k);
     const F3 J = a_r * sum_r + a_m * sum_m;
-    const long long texel = ((long long)k * s.smu + j) * W + n * s.smus + col;
+    const int texel = (k * s.smu + j) * W + n * s.smus + col;
     in.dJ[texel] = to4(J, 1.0f);
   }
 }
