@@ -61,6 +61,12 @@ inline Shape ToShape(const atmo_lut_shape& s) {
   t.snu = s.scattering_nu;
   t.iw = s.irradiance_width;
   t.ih = s.irradiance_height;
+  const int n[kMapCount] = {t.tw, t.th, t.sr, t.smu / 2, t.smus, t.iw, t.ih};
+  for (int i = 0; i < kMapCount; ++i) {
+    volatile float fn = (float)n[i];   // the kernels' 0.5f / float(n), IEEE
+    t.map_c0[i] = 0.5f / fn;
+    t.map_c1[i] = 1.0f - 1.0f / fn;
+  }
   return t;
 }
 

@@ -65,6 +65,18 @@ ATMO_HD F3 fma3(F3 a, F3 b, F3 c) {
   return F3{fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z)};
 }
 ATMO_HD F3 min3(F3 a, float m) { return F3{fminf(a.x, m), fminf(a.y, m), fminf(a.z, m)}; }
+// Quotient with <= 2 ulp error (__fdividef), for ratios of transmittances,
+// which never sit on a LUT boundary.
+ATMO_HD float div_approx(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+ATMO_HD F3 ratio3(F3 a, F3 b) {
+  return F3{div_approx(a.x, b.x), div_approx(a.y, b.y), div_approx(a.z, b.z)};
+}
 ATMO_HD F3 exp3(F3 a) { return F3{expf(a.x), expf(a.y), expf(a.z)}; }
 ATMO_HD float4 to4(F3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
 
@@ -88,10 +100,16 @@ struct ProfileF {
   LayerF layer[2];
 };
 
+// Texture sizes whose texel-centre mapping (functions.glsl:342-344) the
+// kernels evaluate, with the mapping's constants 0.5 / n and 1 - 1 / n.
+enum UnitMapIndex { kMapTW, kMapTH, kMapSR, kMapSMU2, kMapSMUS, kMapIW, kMapIH, kMapCount };
+
 struct Shape {
   int tw, th;             // transmittance W x H
   int sr, smu, smus, snu; // scattering R, MU, MU_S, NU
   int iw, ih;             // irradiance W x H
+  float map_c0[kMapCount];  // 0.5 / n (IEEE, as the kernels would compute it)
+  float map_c1[kMapCount];  // 1 - 1 / n
   ATMO_HD int sw() const { return snu * smus; }
   ATMO_HD long long s_texels() const { return (long long)snu * smus * smu * sr; }
   ATMO_HD int t_texels() const { return tw * th; }
@@ -124,6 +142,10 @@ ATMO_HD float ProfileDensity(const ProfileF& p, float h) {
 ATMO_HD float TexCoordFromUnitRange(float x, int n) {
   // functions.glsl:342-344
   return 0.5f / float(n) + x * (1.0f - 1.0f / float(n));
+}
+// The same with the precomputed constants of the shape.
+ATMO_HD float TexCoord(const Shape& s, int which, float x) {
+  return fmaf(x, s.map_c1[which], s.map_c0[which]);
 }
 
 // A point on a ray: rho^2 = r^2 - Rb^2 kept separately from r so that the
@@ -285,9 +307,9 @@ ATMO_HD TExp FetchTau(const float4* __restrict__ Tau, const TCoords& t) {
 }
 // num / den for values in the m * exp(-e) form.
 ATMO_HD F3 TExpRatio(const TExp& num, const TExp& den) {
-  return F3{num.m.x / den.m.x * expf(den.e.x - num.e.x),
-            num.m.y / den.m.y * expf(den.e.y - num.e.y),
-            num.m.z / den.m.z * expf(den.e.z - num.e.z)};
+  return F3{div_approx(num.m.x, den.m.x) * expf(den.e.x - num.e.x),
+            div_approx(num.m.y, den.m.y) * expf(den.e.y - num.e.y),
+            div_approx(num.m.z, den.m.z) * expf(den.e.z - num.e.z)};
 }
 // Below this the FP32 transmittance loses precision (subnormal range).
 constexpr float kTinyTransmittance = 1e-30f;
@@ -336,7 +358,7 @@ ATMO_HD F3 SegmentTransmittance(const Consts& c, const Shape& s, const float4* T
     return min3(ground ? TExpRatio(x, start.x) : TExpRatio(start.x, x), 1.0f);
   }
   F3 t = FetchTransmittance(T, tc);
-  return min3(ground ? t / start.t : start.t / t, 1.0f);
+  return min3(ground ? ratio3(t, start.t) : ratio3(start.t, t), 1.0f);
 }
 
 // GetTransmittanceToSun (functions.glsl:552-563) at point p with r*mu_s = rmu_s.
@@ -360,7 +382,7 @@ ATMO_HD float UMuSFromMuS(const Consts& c, const Shape& s, float mu_s) {
   float d = rmus > 0.0f ? (c.H * c.H) / (rmus + sq) : sq - rmus;
   float d_min = c.Rt - c.Rb, d_max = c.H;
   float a = (d - d_min) / (d_max - d_min);
-  return TexCoordFromUnitRange(fmaxf(1.0f - a / c.mus_A, 0.0f) / (1.0f + a), s.smus);
+  return TexCoord(s, kMapSMUS, fmaxf(1.0f - a / c.mus_A, 0.0f) / (1.0f + a));
 }
 
 // u_mu when the distance to the ray's boundary is known (d_ray).
@@ -370,12 +392,12 @@ ATMO_HD float UMuFromDistance(const Consts& c, const Shape& s, const RadialPoint
   if (ground) {
     float d_min = p.h, d_max = p.rho;
     float x = d_max == d_min ? 0.0f : clampf((d_ray - d_min) / (d_max - d_min), 0.0f, 1.0f);
-    return 0.5f - 0.5f * TexCoordFromUnitRange(x, half);
+    return 0.5f - 0.5f * TexCoord(s, kMapSMU2, x);
   }
   float d_min = (c.H - p.rho) * (c.H + p.rho) / (c.Rt + p.r);
   float d_max = p.rho + c.H;
   float x = clampf((d_ray - d_min) / (d_max - d_min), 0.0f, 1.0f);
-  return 0.5f + 0.5f * TexCoordFromUnitRange(x, half);
+  return 0.5f + 0.5f * TexCoord(s, kMapSMU2, x);
 }
 
 // u_mu from (rho, r*mu) alone (distance to the ground or to the top).
@@ -473,8 +495,7 @@ ATMO_HD float MiePhase(const Consts& c, float nu) {
 ATMO_HD F3 Irradiance(const Consts& c, const Shape& s, const float4* I, float h, float mu_s) {
   float x_r = h / (c.Rt - c.Rb);
   float x_mu_s = mu_s * 0.5f + 0.5f;
-  return Bilinear(I, s.iw, s.ih, TexCoordFromUnitRange(x_mu_s, s.iw),
-                  TexCoordFromUnitRange(x_r, s.ih));
+  return Bilinear(I, s.iw, s.ih, TexCoord(s, kMapIW, x_mu_s), TexCoord(s, kMapIH, x_r));
 }
 
 ATMO_HD F3 MatVec(const float m[9], F3 v) {

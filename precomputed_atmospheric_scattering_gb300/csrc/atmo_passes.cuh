@@ -307,7 +307,7 @@ ATMO_PASS F3 IndirectIrradiancePartial(const Instance& in, int texel, int order,
   p.rho = ir.rho;
   p.r = ir.r;
   p.h = ir.h;
-  const float u_r = TexCoordFromUnitRange(ir.rho / c.H, s.sr);
+  const float u_r = TexCoord(s, kMapSR, ir.rho / c.H);
   const float u_mu_s = UMuSFromMuS(c, s, mu_s);
   const float dtdp = (kPiF / 32.0f) * (kPiF / 32.0f);
   F3 acc = f3(0.0f);
@@ -361,7 +361,7 @@ ATMO_PASS F3 MultipleScatteringTexel(const Instance& in, long long texel, float*
     // discriminant is invariant along the ray).
     float u_mu = UMuFromDistance(c, s, p, e, ground);
     Lookup4 L = MakeLookup(s, u_nu, UMuSFromMuS(c, s, mu_s_i), u_mu,
-                           TexCoordFromUnitRange(p.rho / c.H, s.sr));
+                           TexCoord(s, kMapSR, p.rho / c.H));
     F3 t = SegmentTransmittance(c, s, in.T, in.Tau, row.rmu, row.delta, p, d, ground, start);
     float w = (i == 0 || i == kMultipleScatteringSamples) ? 0.5f : 1.0f;
     sum = fma3(Scattering4(in.dJ, s, L) * t, dx * w, sum);

@@ -29,7 +29,15 @@ def check(name, gpu, ref, tol, channels=3, report=None):
     mx, p99 = rel_err(gpu, ref, channels)
     if report is not None:
         report[name] = (mx, p99)
-    assert mx <= tol, "%s: max relative error %.3g > %.3g (p99 %.3g)" % (name, mx, tol, p99)
+    where = ""
+    if mx > tol:
+        g = np.asarray(gpu, np.float64)[..., :channels].reshape(-1, channels)
+        r = np.asarray(ref, np.float64)[..., :channels].reshape(-1, channels)
+        q = int(np.argmax(np.abs(g - r).max(axis=1) /
+                          np.maximum(np.abs(r).max(axis=1), 1e-300)))
+        where = " (e.g. texel %d: gpu %s ref %s)" % (q, g[q], r[q])
+    assert mx <= tol, "%s: max relative error %.3g > %.3g (p99 %.3g)%s" % (
+        name, mx, tol, p99, where)
     return mx
 
 
@@ -80,6 +88,10 @@ def check_masked(name, gpu, ref, tol, mask, channels=3, report=None):
     mx = float(e.max()) if e.size else 0.0
     if report is not None:
         report[name] = (mx, int((~mask).sum()))
-    assert mx <= tol, "%s: max relative error %.3g > %.3g on %d robust texels (%d set aside)" % (
-        name, mx, tol, int(mask.sum()), int((~mask).sum()))
+    where = ""
+    if e.size and mx > tol:
+        q = int(np.argmax(e.max(axis=1)))
+        where = " worst texel %d: gpu %s ref %s" % (int(np.flatnonzero(mask)[q]), g[q], r[q])
+    assert mx <= tol, "%s: max relative error %.3g > %.3g on %d robust texels (%d set aside)%s" % (
+        name, mx, tol, int(mask.sum()), int((~mask).sum()), where)
     return mx
