@@ -216,6 +216,24 @@ atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_sh
                             float* scattering, float* single_mie, float* irradiance,
                             atmo_stream stream);
 
+/* The same precomputation without any device-memory allocation, for callers
+   that cannot allocate: plugins of applications that own and pre-reserve all
+   device memory (an engine's texture budget, a framework's caching
+   allocator) and latency-bound code that must avoid cudaMalloc's implicit
+   synchronisation.  No counterpart in the reference (its Init allocates GL
+   textures).  The temporaries live in a fixed 64 MiB device array that every
+   GPU loading this library holds until exit; shapes needing more (the
+   reference's default shape needs ~49 MiB) return ATMO_BUDGET.  All calls
+   share that array: calls whose GPU work overlaps race, so serialise them.
+   The first call on each device looks up the array's device address and
+   should come before any stream capture.  Path: ATMO_PATH_FAST. */
+atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere,
+                                    const atmo_lut_shape* shape,
+                                    unsigned num_scattering_orders, const float lum[9],
+                                    int blend, int combined, float* transmittance,
+                                    float* scattering, float* single_mie, float* irradiance,
+                                    atmo_stream stream);
+
 /* ---- batched precomputation (many atmospheres, uneven shapes/orders) ------- */
 /* Creates a batch of n independent atmospheres, each with its own shape and
    scattering-order count; allocates every instance's LUTs and temporaries. */

@@ -166,6 +166,8 @@ def lib():
                                                      P(C.c_double)],
             "atmo_precompute": [P(Atmosphere), P(LutShape), C.c_uint, P(C.c_float), C.c_int,
                                 C.c_int, C.c_int, vp, vp, vp, vp, vp],
+            "atmo_precompute_noalloc": [P(Atmosphere), P(LutShape), C.c_uint, P(C.c_float),
+                                        C.c_int, C.c_int, vp, vp, vp, vp, vp],
             "atmo_batch_create": [P(Atmosphere), P(LutShape), P(C.c_uint), C.c_uint, C.c_int,
                                   P(vp)],
             "atmo_batch_destroy": [vp],

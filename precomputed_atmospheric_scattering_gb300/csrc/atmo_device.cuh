@@ -388,7 +388,6 @@ ATMO_HD float UMuSFromMuS(const Consts& c, const Shape& s, float mu_s) {
 // u_mu when the distance to the ray's boundary is known (d_ray).
 ATMO_HD float UMuFromDistance(const Consts& c, const Shape& s, const RadialPoint& p,
                               float d_ray, bool ground) {
-  int half = s.smu / 2;
   if (ground) {
     float d_min = p.h, d_max = p.rho;
     float x = d_max == d_min ? 0.0f : clampf((d_ray - d_min) / (d_max - d_min), 0.0f, 1.0f);

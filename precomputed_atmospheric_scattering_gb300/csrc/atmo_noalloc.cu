@@ -1,0 +1,207 @@
+// atmo_noalloc.cu -- atmo_precompute_noalloc: the one-group precomputation of
+// atmo_precompute for callers that must not allocate device memory.
+//
+// Who needs it: code that runs inside a host application which owns and
+// pre-reserves all device memory -- an engine plugin handed only its output
+// textures, or a framework whose caching allocator holds the memory pool, so
+// that a cudaMalloc behind its back fails or fragments the pool -- and code
+// that must not pay cudaMalloc's implicit device synchronisation in a
+// latency-bound loop.  atmo_precompute allocates its temporaries (the delta
+// LUTs, the optical-depth LUT, the set-up tables, the launch descriptors)
+// with cudaMallocAsync; this variant places them in a file-scope device
+// array instead and calls no allocating routine.
+//
+// The array is a fixed kNoAllocScratchBytes (64 MiB) in every GPU that loads
+// this library, held until the process exits.  It fits the reference's
+// default LUT shape (256x64 / 8x32x128x32 / 64x16 needs ~49 MiB); larger
+// shapes are rejected with ATMO_BUDGET.  All calls share it: calls whose GPU
+// work overlaps (concurrent streams, or several host threads) race and must
+// be serialised by the caller.  Nothing needs clearing between calls: every
+// temporary is written in full by an earlier pass of the same call before any
+// pass reads it.
+//
+// Host code cannot use the array's symbol as a device address (it names a
+// host-side stand-in); the device address is obtained once per device with
+// cudaGetSymbolAddress on the first call made with that device current, so
+// that first call should come before any stream capture.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/atmo/atmo.h"
+#include "atmo_consts.h"
+#include "atmo_kernels.h"
+#include "atmo_program.h"
+
+namespace atmo {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+size_t Align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// The scratch layout of one call; offsets in bytes.
+struct NoAllocLayout {
+  size_t instance, worklists, dI, dR, dM, dJ, rows, cols, drows, irows, mus_i, tau, total;
+};
+
+NoAllocLayout Layout(const Shape& s, size_t worklist_ints) {
+  NoAllocLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o = Align256(o + bytes);
+    return at;
+  };
+  const size_t nI = (size_t)s.i_texels(), nS = (size_t)s.s_texels(), nT = (size_t)s.t_texels();
+  L.instance = take(sizeof(Instance));
+  L.worklists = take(worklist_ints * sizeof(int));
+  L.dI = take(nI * 16);
+  L.dR = take(nS * 16);
+  L.dM = take(nS * 16);
+  L.dJ = take(nS * 16);
+  L.rows = take((size_t)s.sr * s.smu * sizeof(TexelRow));
+  L.cols = take((size_t)s.smus * sizeof(TexelCol));
+  L.drows = take((size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow));
+  L.irows = take((size_t)s.ih * sizeof(IrrRow));
+  L.mus_i = take((size_t)s.iw * sizeof(float));
+  L.tau = take(nT * 16);
+  L.total = o;
+  return L;
+}
+
+}  // namespace
+}  // namespace atmo
+
+using namespace atmo;
+
+extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere,
+                                               const atmo_lut_shape* shape,
+                                               unsigned num_scattering_orders,
+                                               const float lum[9], int blend, int combined,
+                                               float* transmittance, float* scattering,
+                                               float* single_mie, float* irradiance,
+                                               atmo_stream stream) {
+  if (!atmosphere || !transmittance || !scattering || !irradiance) {
+    SetError("NULL argument");
+    return ATMO_INVALID_ARG;
+  }
+  if (!combined && !single_mie) {
+    SetError("single_mie is required when combined == 0");
+    return ATMO_INVALID_ARG;
+  }
+  if (num_scattering_orders < 1 || num_scattering_orders > 64) {
+    SetError("num_scattering_orders must be in [1, 64]");
+    return ATMO_INVALID_ARG;
+  }
+  atmo_lut_shape ls = shape ? *shape : DefaultShape();
+  std::string why;
+  if (!ValidShape(ls, &why) || !ValidAtmosphere(*atmosphere, &why)) {
+    SetError(why);
+    return ATMO_INVALID_ARG;
+  }
+  const Shape s = ToShape(ls);
+
+  // The pass sequence of atmosphere/model.cc:1048-1215 for one instance:
+  // each step's work list is {inst = 0; start = 0, tiles}.
+  struct PlannedStep {
+    Pass pass;
+    int order, tiles, smem;
+  };
+  std::vector<PlannedStep> steps;
+  auto add = [&](Pass p, int order) {
+    int smem = p == Pass::kDensity ? DensityFastSmem(s, order) : 0;
+    steps.push_back(PlannedStep{p, order, Tiles(p, s, ATMO_PATH_FAST), smem});
+  };
+  add(Pass::kTables, 0);
+  add(Pass::kTransmittance, 0);
+  add(Pass::kDirect, 0);
+  add(Pass::kSingle, 0);
+  for (unsigned order = 2; order <= num_scattering_orders; ++order) {
+    add(Pass::kDensity, (int)order);
+    add(Pass::kIndirect, (int)order - 1);
+    add(Pass::kMultiple, (int)order);
+  }
+  std::vector<int> wl_ints;
+  for (const PlannedStep& p : steps) {
+    wl_ints.push_back(0);          // inst[0]
+    wl_ints.push_back(0);          // start[0]
+    wl_ints.push_back(p.tiles);    // start[1]
+  }
+  const NoAllocLayout L = Layout(s, wl_ints.size());
+  if (L.total > kNoAllocScratchBytes) {
+    SetError("atmo_precompute_noalloc: this LUT shape needs " + std::to_string(L.total) +
+             " bytes of temporaries, more than the fixed " +
+             std::to_string(kNoAllocScratchBytes) + "-byte scratch array");
+    return ATMO_BUDGET;
+  }
+
+  // Device address of the scratch array on the current device (set-up on the
+  // first call per device).
+  int dev = 0;
+  ATMO_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    SetError("device ordinal out of range");
+    return ATMO_INVALID_ARG;
+  }
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return CudaFail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+      g_noalloc_ptr[dev] = p;
+    }
+    base = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  }
+
+  Instance in;
+  std::memset(&in, 0, sizeof(in));
+  in.c = MakeConsts(*atmosphere, lum);
+  in.s = s;
+  in.T = reinterpret_cast<float4*>(transmittance);
+  in.S = reinterpret_cast<float4*>(scattering);
+  in.M = combined ? nullptr : reinterpret_cast<float4*>(single_mie);
+  in.I = reinterpret_cast<float4*>(irradiance);
+  in.combined = combined ? 1 : 0;
+  in.blend = blend ? 1 : 0;
+  in.dI = reinterpret_cast<float4*>(base + L.dI);
+  in.dR = reinterpret_cast<float4*>(base + L.dR);
+  in.dM = reinterpret_cast<float4*>(base + L.dM);
+  in.dJ = reinterpret_cast<float4*>(base + L.dJ);
+  in.Tau = reinterpret_cast<float4*>(base + L.tau);
+  in.tab.rows = reinterpret_cast<TexelRow*>(base + L.rows);
+  in.tab.cols = reinterpret_cast<TexelCol*>(base + L.cols);
+  in.tab.drows = reinterpret_cast<DensityRow*>(base + L.drows);
+  in.tab.irows = reinterpret_cast<IrrRow*>(base + L.irows);
+  in.tab.mus_i = reinterpret_cast<float*>(base + L.mus_i);
+
+  // Launch descriptors into the scratch array (pageable copies: the host
+  // buffers may be released once the calls return).
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  ATMO_CUDA_TRY(cudaMemcpyAsync(base + L.instance, &in, sizeof(in), cudaMemcpyHostToDevice, st));
+  ATMO_CUDA_TRY(cudaMemcpyAsync(base + L.worklists, wl_ints.data(), wl_ints.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, st));
+  const Instance* d_in = reinterpret_cast<const Instance*>(base + L.instance);
+  const int* d_wl = reinterpret_cast<const int*>(base + L.worklists);
+  for (size_t i = 0; i < steps.size(); ++i) {
+    WorkList wl;
+    wl.inst = d_wl + 3 * i;
+    wl.start = d_wl + 3 * i + 1;
+    wl.count = 1;
+    cudaError_t e = LaunchPass(steps[i].pass, steps[i].order, steps[i].smem, d_in, wl,
+                               steps[i].tiles, ATMO_PATH_FAST, st);
+    if (e != cudaSuccess) return CudaFail(e, "kernel launch");
+  }
+  return ATMO_OK;
+}

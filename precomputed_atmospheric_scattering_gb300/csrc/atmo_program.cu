@@ -234,40 +234,40 @@ atmo_status Program::TimeSteps(cudaStream_t st, std::vector<float>* ms) {
   return ATMO_OK;
 }
 
-atmo_status Program::LaunchStep(size_t i, cudaStream_t st) {
-  {
-    const Step& step = steps_[i];
-    const WorkList& wl = wls_[step.wl];
-    cudaError_t e = cudaSuccess;
-    switch (step.pass) {
-      case Pass::kTables: e = LaunchTables(d_slots_, wl, step.tiles, st); break;
-      case Pass::kTransmittance: e = LaunchTransmittance(d_slots_, wl, step.tiles, st); break;
-      case Pass::kDirect: e = LaunchDirectIrradiance(d_slots_, wl, step.tiles, st); break;
-      case Pass::kSingle: e = LaunchSingleScattering(d_slots_, wl, step.tiles, st); break;
-      case Pass::kDensity:
-        e = path == ATMO_PATH_FAST
-                ? LaunchDensityFast(d_slots_, wl, step.tiles, step.order, step.smem, st)
-                : LaunchDensityPlain(d_slots_, wl, step.tiles, step.order, st);
-        break;
-      case Pass::kIndirect:
-        e = LaunchIndirectIrradiance(d_slots_, wl, step.tiles, step.order, st);
-        break;
-      case Pass::kMultiple:
-        e = path == ATMO_PATH_FAST ? LaunchMultipleFast(d_slots_, wl, step.tiles, st)
-                                   : LaunchMultiplePlain(d_slots_, wl, step.tiles, st);
-        break;
-      case Pass::kToHalf: {
-        // One slot per step: convert its scattering (and single-Mie) outputs.
-        int m = blob_[wl_offsets_[step.wl].first];
-        const Instance& in = slots[m];
-        if (in.S_half) e = LaunchToHalf(in.S, in.S_half, in.s.s_texels(), st);
-        if (e == cudaSuccess && in.M && in.M_half)
-          e = LaunchToHalf(in.M, in.M_half, in.s.s_texels(), st);
-        break;
-      }
-    }
-    if (e != cudaSuccess) return CudaFail(e, "kernel launch");
+cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, WorkList wl,
+                       int tiles, atmo_path path, cudaStream_t st) {
+  switch (pass) {
+    case Pass::kTables: return LaunchTables(insts, wl, tiles, st);
+    case Pass::kTransmittance: return LaunchTransmittance(insts, wl, tiles, st);
+    case Pass::kDirect: return LaunchDirectIrradiance(insts, wl, tiles, st);
+    case Pass::kSingle: return LaunchSingleScattering(insts, wl, tiles, st);
+    case Pass::kDensity:
+      return path == ATMO_PATH_FAST ? LaunchDensityFast(insts, wl, tiles, order, smem, st)
+                                    : LaunchDensityPlain(insts, wl, tiles, order, st);
+    case Pass::kIndirect: return LaunchIndirectIrradiance(insts, wl, tiles, order, st);
+    case Pass::kMultiple:
+      return path == ATMO_PATH_FAST ? LaunchMultipleFast(insts, wl, tiles, st)
+                                    : LaunchMultiplePlain(insts, wl, tiles, st);
+    case Pass::kToHalf: return cudaErrorInvalidValue;   // handled by the program
   }
+  return cudaErrorInvalidValue;
+}
+
+atmo_status Program::LaunchStep(size_t i, cudaStream_t st) {
+  const Step& step = steps_[i];
+  const WorkList& wl = wls_[step.wl];
+  cudaError_t e = cudaSuccess;
+  if (step.pass == Pass::kToHalf) {
+    // One slot per step: convert its scattering (and single-Mie) outputs.
+    int m = blob_[wl_offsets_[step.wl].first];
+    const Instance& in = slots[m];
+    if (in.S_half) e = LaunchToHalf(in.S, in.S_half, in.s.s_texels(), st);
+    if (e == cudaSuccess && in.M && in.M_half)
+      e = LaunchToHalf(in.M, in.M_half, in.s.s_texels(), st);
+  } else {
+    e = LaunchPass(step.pass, step.order, step.smem, d_slots_, wl, step.tiles, path, st);
+  }
+  if (e != cudaSuccess) return CudaFail(e, "kernel launch");
   return ATMO_OK;
 }
 

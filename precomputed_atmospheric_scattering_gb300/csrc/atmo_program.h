@@ -92,6 +92,10 @@ class Program {
 };
 
 int Tiles(Pass pass, const Shape& s, atmo_path path);
+// Launches one pass over the instances of `wl` (device pointers); kToHalf is
+// not a pass kernel and returns cudaErrorInvalidValue.
+cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, WorkList wl,
+                       int tiles, atmo_path path, cudaStream_t st);
 
 }  // namespace atmo
 
