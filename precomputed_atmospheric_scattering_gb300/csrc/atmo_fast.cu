@@ -199,8 +199,222 @@ cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int
   return cudaGetLastError();
 }
 
-cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, cudaStream_t st) {
-  return LaunchMultiplePlain(insts, wl, tiles, st);
+// ---------------------------------------------------------------------------
+// Multiple scattering, restructured (functions.glsl:1268-1308).
+//
+// Every quantity of a quadrature sample but mu_s depends only on the texel's
+// row (r-slice k, mu-row j): the sample's r and mu, hence the (y, z) position
+// of its 4D lookup, and the transmittance from the texel to the sample.  A
+// block owns whole rows; it computes their samples once (RaySample), then,
+// per sample, interpolates the density LUT in (mu, r) at the sample into a
+// line of W = NU x MU_S columns in shared memory.  A texel's lookup reduces to
+// its own mu_s mapping and a bilinear (mu_s, nu) interpolation of 4 columns
+// of that line.  Lines are built G samples at a time, double-buffered, so a
+// stage needs one barrier.
+// ---------------------------------------------------------------------------
+constexpr int kMultipleFastThreads = 256;
+constexpr int kMultipleFastMaxCols = 4;   // texel columns per thread (W <= 1024)
+constexpr int kRaySamples = kMultipleScatteringSamples + 1;
+
+struct __align__(16) RaySample {
+  int r00, r01, r10, r11;    // element offsets of the LUT rows (k0 j0, k0 j1, k1 j0, k1 j1)
+  float w00, w01, w10, w11;  // their bilinear weights in (mu, r)
+  float tx, ty, tz;          // transmittance texel -> sample x dx x trapezoid weight
+  float d;                   // distance from the texel's point along its ray
+  float inv_r;               // 1 / r at the sample
+  float pad[3];
+};
+
+struct MultipleFastDims {
+  int rows;    // LUT rows per block
+  int group;   // samples per line stage
+};
+__host__ __device__ inline MultipleFastDims MultipleDims(const Shape& s) {
+  const int W = s.sw();
+  int rows = kMultipleFastThreads / W;
+  rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
+  // Two line buffers of group x rows x W float4 within 32 KB.
+  int group = 32768 / (2 * 16 * rows * W);
+  group = group < 1 ? 1 : (group > 4 ? 4 : group);
+  return MultipleFastDims{rows, group};
+}
+bool MultipleFastFits(const Shape& s) {
+  return s.sw() <= kMultipleFastThreads * kMultipleFastMaxCols;
+}
+int MultipleFastTiles(const Shape& s) {
+  const int rows = MultipleDims(s).rows;
+  return (s.sr * s.smu + rows - 1) / rows;
+}
+int MultipleFastSmem(const Shape& s) {
+  const MultipleFastDims d = MultipleDims(s);
+  return d.rows * kRaySamples * (int)sizeof(RaySample) + 2 * d.group * d.rows * s.sw() * 16;
+}
+
+// Sample i of the ray of LUT row `rowi` (the per-sample part of
+// MultipleScatteringTexel that does not depend on mu_s or nu).
+__device__ RaySample MakeRaySample(const Instance& in, int rowi, int i) {
+  const Consts& c = in.c;
+  const Shape& s = in.s;
+  const TexelRow row = in.tab.rows[rowi];
+  const bool ground = row.ground != 0;
+  const float dx = row.d / float(kMultipleScatteringSamples);
+  const float d = float(i) * dx;
+  const float e = float(kMultipleScatteringSamples - i) * dx;
+  const RadialPoint p = PointFromRho2(c, RayRho2(row, d, e));
+  const float u_mu = UMuFromDistance(c, s, p, e, ground);
+  const float u_r = TexCoord(s, kMapSR, p.rho / c.H);
+  const TStart start = MakeTStart(c, s, in.T, in.Tau, row.rho, row.r,
+                                  ground ? -row.rmu : row.rmu, row.delta);
+  const F3 t = SegmentTransmittance(c, s, in.T, in.Tau, row.rmu, row.delta, p, d, ground, start);
+  const float w = (i == 0 || i == kMultipleScatteringSamples) ? 0.5f : 1.0f;
+  const float Y = u_mu * float(s.smu) - 0.5f, Z = u_r * float(s.sr) - 0.5f;
+  const float fy = floorf(Y), fz = floorf(Z);
+  const float b = Y - fy, cz = Z - fz;
+  const int j0 = ClampIdx((int)fy, s.smu), j1 = ClampIdx((int)fy + 1, s.smu);
+  const int k0 = ClampIdx((int)fz, s.sr), k1 = ClampIdx((int)fz + 1, s.sr);
+  const int W = s.sw();
+  RaySample rs;
+  rs.r00 = (k0 * s.smu + j0) * W;
+  rs.r01 = (k0 * s.smu + j1) * W;
+  rs.r10 = (k1 * s.smu + j0) * W;
+  rs.r11 = (k1 * s.smu + j1) * W;
+  rs.w00 = (1.0f - b) * (1.0f - cz);
+  rs.w01 = b * (1.0f - cz);
+  rs.w10 = (1.0f - b) * cz;
+  rs.w11 = b * cz;
+  const float dw = dx * w;
+  rs.tx = t.x * dw;
+  rs.ty = t.y * dw;
+  rs.tz = t.z * dw;
+  rs.d = d;
+  rs.inv_r = 1.0f / p.r;
+  rs.pad[0] = rs.pad[1] = rs.pad[2] = 0.0f;
+  return rs;
+}
+
+template <int kCols>
+__device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local, float4* smem) {
+  const Shape s = in.s;
+  const Consts& c = in.c;
+  const MultipleFastDims dims = MultipleDims(s);
+  const int W = s.sw(), R = dims.rows, G = dims.group;
+  const int rows_total = s.sr * s.smu;
+  const int row0 = local * R;
+  RaySample* samp = reinterpret_cast<RaySample*>(smem);                 // [R][kRaySamples]
+  float4* line = smem + R * kRaySamples * (int)(sizeof(RaySample) / 16);   // [2][G][R][W]
+
+  for (int e = threadIdx.x; e < R * kRaySamples; e += kMultipleFastThreads) {
+    const int rr = e / kRaySamples, i = e - rr * kRaySamples;
+    if (row0 + rr < rows_total) samp[e] = MakeRaySample(in, row0 + rr, i);
+  }
+
+  // This thread's row within the tile and its texel columns x_t + 256 m.
+  const int rr = kCols == 1 ? (int)threadIdx.x / W : 0;
+  const int x_t = kCols == 1 ? (int)threadIdx.x - rr * W : (int)threadIdx.x;
+  const int rowi = row0 + rr;
+  const bool active = rr < R && rowi < rows_total;
+  const float smus_f = float(s.smus);
+  const int nmax = W - 1;
+  float rmu_s[kCols], nu[kCols], xb[kCols], lnu[kCols];
+  F3 acc[kCols];
+  if (active) {
+    const TexelRow row = in.tab.rows[rowi];
+#pragma unroll
+    for (int m = 0; m < kCols; ++m) {
+      const int x = min(x_t + m * kMultipleFastThreads, nmax);
+      const int n = x / s.smus, col = x - n * s.smus;
+      const TexelAngles ang = MakeAngles(s, row, in.tab.cols[col], n);
+      rmu_s[m] = row.r * ang.mu_s;
+      nu[m] = ang.nu;
+      const float tex_coord_x = (ang.nu + 1.0f) * 0.5f * float(s.snu - 1);
+      const float tex_x = floorf(tex_coord_x);
+      lnu[m] = tex_coord_x - tex_x;
+      xb[m] = tex_x * smus_f - 0.5f;
+      acc[m] = f3(0.0f);
+    }
+  }
+  __syncthreads();
+
+  const int line_stride = G * R * W;
+  const int stages = (kRaySamples + G - 1) / G;
+  for (int stage = 0; stage < stages; ++stage) {
+    float4* buf = line + (stage & 1) * line_stride;
+    const int first = stage * G;
+    const int count = min(G, kRaySamples - first);
+    if (active) {
+      for (int g = 0; g < count; ++g) {
+        const RaySample& sm = samp[rr * kRaySamples + first + g];
+        float4* out = buf + (g * R + rr) * W;
+#pragma unroll
+        for (int m = 0; m < kCols; ++m) {
+          const int x = x_t + m * kMultipleFastThreads;
+          if (kCols > 1 && x >= W) break;
+          const float4 a = __ldg(in.dJ + sm.r00 + x), b = __ldg(in.dJ + sm.r01 + x);
+          const float4 p = __ldg(in.dJ + sm.r10 + x), q = __ldg(in.dJ + sm.r11 + x);
+          out[x] = make_float4(
+              fmaf(q.x, sm.w11, fmaf(p.x, sm.w10, fmaf(b.x, sm.w01, a.x * sm.w00))),
+              fmaf(q.y, sm.w11, fmaf(p.y, sm.w10, fmaf(b.y, sm.w01, a.y * sm.w00))),
+              fmaf(q.z, sm.w11, fmaf(p.z, sm.w10, fmaf(b.z, sm.w01, a.z * sm.w00))), 0.0f);
+        }
+      }
+    }
+    __syncthreads();
+    if (active) {
+      for (int g = 0; g < count; ++g) {
+        const RaySample& sm = samp[rr * kRaySamples + first + g];
+        const float4* L = buf + (g * R + rr) * W;
+#pragma unroll
+        for (int m = 0; m < kCols; ++m) {
+          if (kCols > 1 && x_t + m * kMultipleFastThreads >= W) break;
+          const float mu_s_i = clampf(fmaf(sm.d, nu[m], rmu_s[m]) * sm.inv_r, -1.0f, 1.0f);
+          const float x0 = fmaf(UMuSFromMuS(c, s, mu_s_i), smus_f, xb[m]);
+          const float fx = floorf(x0);
+          const float a = x0 - fx;
+          const int i0 = (int)fx;
+          const int c0 = min(max(i0, 0), nmax), c1 = min(max(i0 + 1, 0), nmax);
+          const int c2 = min(max(i0 + s.smus, 0), nmax), c3 = min(max(i0 + s.smus + 1, 0), nmax);
+          const float l1 = lnu[m], l0 = 1.0f - l1;
+          const float v0 = (1.0f - a) * l0, v1 = a * l0, v2 = (1.0f - a) * l1, v3 = a * l1;
+          const float4 t0 = L[c0], t1 = L[c1], t2 = L[c2], t3 = L[c3];
+          const F3 S{fmaf(t3.x, v3, fmaf(t2.x, v2, fmaf(t1.x, v1, t0.x * v0))),
+                     fmaf(t3.y, v3, fmaf(t2.y, v2, fmaf(t1.y, v1, t0.y * v0))),
+                     fmaf(t3.z, v3, fmaf(t2.z, v2, fmaf(t1.z, v1, t0.z * v0)))};
+          acc[m] = fma3(S, F3{sm.tx, sm.ty, sm.tz}, acc[m]);
+        }
+      }
+    }
+  }
+
+  if (!active) return;
+#pragma unroll
+  for (int m = 0; m < kCols; ++m) {
+    const int x = x_t + m * kMultipleFastThreads;
+    if (kCols > 1 && x >= W) break;
+    const int texel = rowi * W + x;
+    in.dR[texel] = to4(acc[m], 1.0f);   // delta multiple aliases delta Rayleigh
+    const F3 add = MatVec(c.lum, acc[m]) * (1.0f / RayleighPhase(c, nu[m]));
+    const float4 o = in.S[texel];
+    in.S[texel] = make_float4(o.x + add.x, o.y + add.y, o.z + add.z, o.w);
+  }
+}
+
+__global__ void __launch_bounds__(kMultipleFastThreads)
+k_multiple_fast(const Instance* __restrict__ insts, WorkList wl) {
+  extern __shared__ float4 smem[];
+  int local;
+  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
+  if (in.s.sw() <= kMultipleFastThreads) {
+    MultipleFastBlock<1>(in, local, smem);
+  } else {
+    MultipleFastBlock<kMultipleFastMaxCols>(in, local, smem);
+  }
+}
+
+cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, int smem_bytes,
+                               cudaStream_t st) {
+  // smem_bytes: the largest MultipleFastSmem of the work list's instances.
+  k_multiple_fast<<<tiles, kMultipleFastThreads, (size_t)smem_bytes, st>>>(insts, wl);
+  return cudaGetLastError();
 }
 
 __global__ void k_to_half(const float4* __restrict__ src, __half2* __restrict__ dst, long long n) {

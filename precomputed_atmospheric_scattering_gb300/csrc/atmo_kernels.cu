@@ -1,6 +1,8 @@
-// atmo_kernels.cu -- sm_103a kernels of the plain precomputation path: one
-// launch per pass of atmosphere/model.cc:1048-1215 covering every instance of
-// a work list (a single model is a work list of one).
+// atmo_kernels.cu -- sm_103a kernels of the transmittance and irradiance
+// passes: one launch per pass of atmosphere/model.cc:1048-1215 covering every
+// instance of a work list (a single model is a work list of one).  IEEE
+// division and square root: their lookups start from LUT rows and columns of
+// the set-up tables and must land on texel centres and LUT edges exactly.
 #include "atmo_kernels.h"
 #include "atmo_passes.cuh"
 
@@ -51,26 +53,6 @@ k_direct_irradiance(const Instance* __restrict__ insts, WorkList wl) {
   if (e < in.s.sr * kDensityThetaSamples) in.tab.drows[e].t_ground = GroundRowTransmittance(in, e);
 }
 
-__global__ void __launch_bounds__(kTexelThreads)
-k_single_scattering(const Instance* __restrict__ insts, WorkList wl) {
-  int local;
-  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
-  long long texel = (long long)local * kTexelThreads + threadIdx.x;
-  if (texel >= in.s.s_texels()) return;
-  F3 ray, mie;
-  SingleScatteringTexel(in, texel, &ray, &mie);
-  StoreSingleScattering(in, texel, ray, mie);
-}
-
-__global__ void __launch_bounds__(kTexelThreads)
-k_density_plain(const Instance* __restrict__ insts, WorkList wl, int order) {
-  int local;
-  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
-  long long texel = (long long)local * kTexelThreads + threadIdx.x;
-  if (texel >= in.s.s_texels()) return;
-  in.dJ[texel] = to4(ScatteringDensityTexel(in, texel, order), 1.0f);
-}
-
 // Indirect irradiance: one warp per texel, lanes over the 64 phi samples.
 __global__ void __launch_bounds__(kIndirectThreads)
 k_indirect_irradiance(const Instance* __restrict__ insts, WorkList wl, int order) {
@@ -94,20 +76,6 @@ k_indirect_irradiance(const Instance* __restrict__ insts, WorkList wl, int order
   }
 }
 
-__global__ void __launch_bounds__(kTexelThreads)
-k_multiple_plain(const Instance* __restrict__ insts, WorkList wl) {
-  int local;
-  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
-  long long texel = (long long)local * kTexelThreads + threadIdx.x;
-  if (texel >= in.s.s_texels()) return;
-  float nu;
-  F3 dm = MultipleScatteringTexel(in, texel, &nu);
-  in.dR[texel] = to4(dm, 1.0f);   // delta multiple aliases delta Rayleigh
-  F3 add = MatVec(in.c.lum, dm) * (1.0f / RayleighPhase(in.c, nu));
-  float4 o = in.S[texel];
-  in.S[texel] = make_float4(o.x + add.x, o.y + add.y, o.z + add.z, o.w);
-}
-
 // ---------------------------------------------------------------------------
 // Host-side launchers.
 // ---------------------------------------------------------------------------
@@ -120,25 +88,9 @@ cudaError_t LaunchDirectIrradiance(const Instance* insts, WorkList wl, int tiles
   k_direct_irradiance<<<tiles, kTexelThreads, 0, st>>>(insts, wl);
   return cudaGetLastError();
 }
-cudaError_t LaunchSingleScattering(const Instance* insts, WorkList wl, int tiles,
-                                   cudaStream_t st) {
-  k_single_scattering<<<tiles, kTexelThreads, 0, st>>>(insts, wl);
-  return cudaGetLastError();
-}
-cudaError_t LaunchDensityPlain(const Instance* insts, WorkList wl, int tiles, int order,
-                               cudaStream_t st) {
-  k_density_plain<<<tiles, kTexelThreads, 0, st>>>(insts, wl, order);
-  return cudaGetLastError();
-}
 cudaError_t LaunchIndirectIrradiance(const Instance* insts, WorkList wl, int tiles, int order,
                                      cudaStream_t st) {
   k_indirect_irradiance<<<tiles, kIndirectThreads, 0, st>>>(insts, wl, order);
   return cudaGetLastError();
 }
-cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
-                                cudaStream_t st) {
-  k_multiple_plain<<<tiles, kTexelThreads, 0, st>>>(insts, wl);
-  return cudaGetLastError();
-}
-
 }  // namespace atmo

@@ -26,7 +26,11 @@ int DensityFastTiles(const Shape& s);
 int DensityFastSmem(const Shape& s, int order);
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
                               int smem_bytes, cudaStream_t st);
-cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles,
+// The row-restructured multiple-scattering kernel needs W = NU x MU_S <= 1024.
+bool MultipleFastFits(const Shape& s);
+int MultipleFastTiles(const Shape& s);
+int MultipleFastSmem(const Shape& s);
+cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, int smem_bytes,
                                cudaStream_t st);
 // Final conversion of the scattering accumulators to half precision.
 cudaError_t LaunchToHalf(const float4* src, void* dst, long long n, cudaStream_t st);

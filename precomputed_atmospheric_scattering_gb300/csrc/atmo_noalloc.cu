@@ -116,11 +116,13 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
   struct PlannedStep {
     Pass pass;
     int order, tiles, smem;
+    atmo_path path;
   };
   std::vector<PlannedStep> steps;
   auto add = [&](Pass p, int order) {
-    int smem = p == Pass::kDensity ? DensityFastSmem(s, order) : 0;
-    steps.push_back(PlannedStep{p, order, Tiles(p, s, ATMO_PATH_FAST), smem});
+    const atmo_path path = PassPath(p, s, ATMO_PATH_FAST);
+    steps.push_back(
+        PlannedStep{p, order, Tiles(p, s, path), SharedBytes(p, s, order, path), path});
   };
   add(Pass::kTables, 0);
   add(Pass::kTransmittance, 0);
@@ -200,7 +202,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     wl.start = d_wl + 3 * i + 1;
     wl.count = 1;
     cudaError_t e = LaunchPass(steps[i].pass, steps[i].order, steps[i].smem, d_in, wl,
-                               steps[i].tiles, ATMO_PATH_FAST, st);
+                               steps[i].tiles, steps[i].path, st);
     if (e != cudaSuccess) return CudaFail(e, "kernel launch");
   }
   return ATMO_OK;

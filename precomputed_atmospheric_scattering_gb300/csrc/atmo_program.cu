@@ -87,6 +87,19 @@ size_t Storage::Bytes() const {
 // ---------------------------------------------------------------------------
 // Program
 // ---------------------------------------------------------------------------
+atmo_path PassPath(Pass pass, const Shape& s, atmo_path path) {
+  if (pass == Pass::kMultiple && path == ATMO_PATH_FAST && !MultipleFastFits(s))
+    return ATMO_PATH_PLAIN;
+  return path;
+}
+
+int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path) {
+  if (path != ATMO_PATH_FAST) return 0;
+  if (pass == Pass::kDensity) return DensityFastSmem(s, order);
+  if (pass == Pass::kMultiple) return MultipleFastSmem(s);
+  return 0;
+}
+
 int Tiles(Pass pass, const Shape& s, atmo_path path) {
   auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
   switch (pass) {
@@ -97,7 +110,8 @@ int Tiles(Pass pass, const Shape& s, atmo_path path) {
     case Pass::kDensity:
       return path == ATMO_PATH_FAST ? DensityFastTiles(s) : cdiv(s.s_texels(), kTexelThreads);
     case Pass::kIndirect: return cdiv(s.i_texels(), kIndirectTexelsPerTile);
-    case Pass::kMultiple: return cdiv(s.s_texels(), kTexelThreads);
+    case Pass::kMultiple:
+      return path == ATMO_PATH_FAST ? MultipleFastTiles(s) : cdiv(s.s_texels(), kTexelThreads);
     case Pass::kToHalf: return cdiv(s.s_texels(), 256);
   }
   return 0;
@@ -113,19 +127,28 @@ Program::~Program() {
 }
 
 int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles,
-                         int* smem) {
+                         int* smem, atmo_path* step_path) {
   std::vector<int> inst, start;
+  auto takes_part = [&](int m) {
+    if ((pass == Pass::kDensity || pass == Pass::kMultiple) && orders[m] < (unsigned)order)
+      return false;
+    if (pass == Pass::kIndirect && orders[m] < (unsigned)order + 1) return false;
+    return true;
+  };
+  // One kernel variant per launch: the fast one only if every member takes it.
+  atmo_path p = path;
+  for (int m : members)
+    if (takes_part(m) && PassPath(pass, slots[m].s, path) != path) p = ATMO_PATH_PLAIN;
+  if (step_path) *step_path = p;
   int t = 0;
   if (smem) *smem = 0;
   for (int m : members) {
-    if ((pass == Pass::kDensity || pass == Pass::kMultiple) && orders[m] < (unsigned)order)
-      continue;
-    if (pass == Pass::kIndirect && orders[m] < (unsigned)order + 1) continue;
+    if (!takes_part(m)) continue;
     inst.push_back(m);
     start.push_back(t);
-    t += Tiles(pass, slots[m].s, path);
-    if (smem && pass == Pass::kDensity && path == ATMO_PATH_FAST) {
-      int b = DensityFastSmem(slots[m].s, order);
+    t += Tiles(pass, slots[m].s, p);
+    if (smem) {
+      int b = SharedBytes(pass, slots[m].s, order, p);
       *smem = b > *smem ? b : *smem;
     }
   }
@@ -142,8 +165,9 @@ int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, 
 void Program::AddStage(const std::vector<int>& members, bool transmittance_only) {
   auto add = [&](Pass p, int order) {
     int tiles = 0, smem = 0;
-    int wl = AddWorkList(members, p, order, &tiles, &smem);
-    if (wl >= 0 && tiles > 0) steps_.push_back(Step{p, order, wl, tiles, smem});
+    atmo_path step_path = path;
+    int wl = AddWorkList(members, p, order, &tiles, &smem, &step_path);
+    if (wl >= 0 && tiles > 0) steps_.push_back(Step{p, order, wl, tiles, smem, step_path});
   };
   if (transmittance_only) {
     add(Pass::kTransmittance, 0);
@@ -166,7 +190,7 @@ void Program::AddToHalf(const std::vector<int>& members) {
   for (int m : members) {
     int tiles = 0;
     int wl = AddWorkList({m}, Pass::kToHalf, 0, &tiles);
-    if (wl >= 0) steps_.push_back(Step{Pass::kToHalf, 0, wl, tiles, 0});
+    if (wl >= 0) steps_.push_back(Step{Pass::kToHalf, 0, wl, tiles, 0, path});
   }
 }
 
@@ -246,7 +270,7 @@ cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, Wo
                                     : LaunchDensityPlain(insts, wl, tiles, order, st);
     case Pass::kIndirect: return LaunchIndirectIrradiance(insts, wl, tiles, order, st);
     case Pass::kMultiple:
-      return path == ATMO_PATH_FAST ? LaunchMultipleFast(insts, wl, tiles, st)
+      return path == ATMO_PATH_FAST ? LaunchMultipleFast(insts, wl, tiles, smem, st)
                                     : LaunchMultiplePlain(insts, wl, tiles, st);
     case Pass::kToHalf: return cudaErrorInvalidValue;   // handled by the program
   }
@@ -265,7 +289,7 @@ atmo_status Program::LaunchStep(size_t i, cudaStream_t st) {
     if (e == cudaSuccess && in.M && in.M_half)
       e = LaunchToHalf(in.M, in.M_half, in.s.s_texels(), st);
   } else {
-    e = LaunchPass(step.pass, step.order, step.smem, d_slots_, wl, step.tiles, path, st);
+    e = LaunchPass(step.pass, step.order, step.smem, d_slots_, wl, step.tiles, step.path, st);
   }
   if (e != cudaSuccess) return CudaFail(e, "kernel launch");
   return ATMO_OK;

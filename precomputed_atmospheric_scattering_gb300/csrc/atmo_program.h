@@ -47,7 +47,8 @@ struct Step {
   int order;      // scattering order of density / multiple; order-1 for indirect
   int wl;         // work-list index
   int tiles;      // blocks of the launch
-  int smem;       // dynamic shared memory bytes (fast density)
+  int smem;       // dynamic shared memory bytes (fast kernels)
+  atmo_path path; // kernel variant of this launch
 };
 
 // A program: a sequence of stages; a stage runs the full precomputation of a
@@ -77,7 +78,7 @@ class Program {
 
  private:
   int AddWorkList(const std::vector<int>& members, Pass pass, int order, int* tiles,
-                  int* smem = nullptr);
+                  int* smem = nullptr, atmo_path* step_path = nullptr);
   std::vector<Step> steps_;
   std::vector<int> blob_;              // inst[] then start[] of every work list
   std::vector<std::pair<int, int>> wl_offsets_;  // (offset, count)
@@ -91,7 +92,14 @@ class Program {
   bool finalized_ = false;
 };
 
+// The kernel variant that runs `pass` for shape s when `path` is requested:
+// the fast multiple-scattering kernel holds a LUT row of NU x MU_S texels in
+// shared memory and takes shapes up to 1024 of them.
+atmo_path PassPath(Pass pass, const Shape& s, atmo_path path);
+// Blocks and dynamic shared memory of `pass` for shape s under the variant
+// `path` (as PassPath returns it).
 int Tiles(Pass pass, const Shape& s, atmo_path path);
+int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path);
 // Launches one pass over the instances of `wl` (device pointers); kToHalf is
 // not a pass kernel and returns cudaErrorInvalidValue.
 cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, WorkList wl,

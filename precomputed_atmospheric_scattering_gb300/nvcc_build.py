@@ -17,13 +17,15 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
           "-Xptxas", "-warn-spills"]
 # Per-unit flags: the FP64 set-up tables round like the reference's CPU model.
-# The slab density kernel uses the approximate (<= 2 ulp) single-precision
-# division and square root (its lookup coordinates come from the FP64 tables);
-# the other FP32 kernels keep IEEE division, whose exact results put lookups
-# on texel centres and LUT edges exactly where the reference does.
+# The ray-marching kernels (atmo_rays.cu) and the slab density kernel use the
+# approximate (<= 2 ulp) single-precision division and square root; the
+# transmittance and irradiance kernels keep IEEE division, whose exact results
+# put lookups that start on LUT rows on texel centres and edges exactly where
+# the reference does.
 UNIT_FLAGS = {"atmo_tables.cu": ["--fmad=false"],
+              "atmo_rays.cu": ["--prec-div=false", "--prec-sqrt=false"],
               "atmo_fast.cu": ["--prec-div=false", "--prec-sqrt=false"]}
-UNITS = ["atmo_tables.cu", "atmo_kernels.cu", "atmo_fast.cu", "atmo_program.cu",
+UNITS = ["atmo_tables.cu", "atmo_kernels.cu", "atmo_rays.cu", "atmo_fast.cu", "atmo_program.cu",
          "atmo_capi.cu", "atmo_noalloc.cu"]
 
 
