@@ -24,166 +24,242 @@ constexpr int kDensityFastThreads = 256;
 
 int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
 
-// Shared memory of one block, bytes: per staged species a [16][NU] float4
-// table (L.x, L.y, L.z, D.x) and a [16][NU] float2 table (D.y, D.z), where
-// D = L[n + 1] - L[n] is the slope towards the next nu node; then the bottom
-// row of the irradiance LUT; then a float temporary per table entry.
-int DensityFastSmem(const Shape& s, int order) {
-  const int species = order == 2 ? 2 : 1;
-  return species * kDensityThetaSamples * s.snu *
-             (int)(sizeof(float4) + sizeof(float2) + sizeof(float)) +
-         s.iw * (int)sizeof(float4);
+// Piecewise-linear functions staged in shared memory are stored per node as
+// the midpoint of the segment to the next node and the segment's slope (the
+// slope is 0 at the last node), so that a lookup is mid + w slope with w in
+// [-0.5, 0.5].  The segment is found by rounding rather than flooring: adding
+// 1.5 x 2^23 to x (|x| < 2^22) leaves round(x) in the sum's low mantissa bits,
+// ties to even, and (sum - 1.5 x 2^23) is round(x) as a float, exactly.  With
+// x = node coordinate - 0.5 >= -0.5 that selects the segment [n, n + 1]
+// holding the coordinate (a coordinate on a node may take either segment;
+// both give the node's value).  The sum's bit pattern, times the entry size,
+// plus a row offset that cancels the constant's exponent bits (mod 2^32), is
+// the entry's shared-memory address.
+constexpr float kRoundMagic = 12582912.0f;
+constexpr uint32_t kRoundMagicBits = 0x4B400000u;
+
+// One node entry: mid.xyz, slope.x | slope.y, slope.z, -, -.
+constexpr int kNodeBytes = 32;
+
+template <int kOffset>
+__device__ __forceinline__ float4 LoadShared4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4+%5];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr), "n"(kOffset));
+  return v;
+}
+template <int kOffset>
+__device__ __forceinline__ float2 LoadShared2(uint32_t addr) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(kOffset));
+  return v;
+}
+__device__ __forceinline__ void StoreNode(float4* entry, float4 v, float4 next) {
+  const float dx = next.x - v.x, dy = next.y - v.y, dz = next.z - v.z;
+  entry[0] = make_float4(fmaf(0.5f, dx, v.x), fmaf(0.5f, dy, v.y), fmaf(0.5f, dz, v.z), dx);
+  entry[1] = make_float4(dy, dz, 0.0f, 0.0f);
+}
+// The staged function at node coordinate u + 0.5 (u >= -0.5) of the table
+// whose entries (kStride bytes apart, the function's at byte kOffset) start
+// at row_adj + kRoundMagicBits kStride.
+template <int kStride, int kOffset>
+__device__ __forceinline__ F3 EvalNodes(float u, float t, uint32_t row_adj) {
+  const float w = u - (t - kRoundMagic);
+  const uint32_t a = (uint32_t)__float_as_int(t) * (uint32_t)kStride + row_adj;
+  const float4 p = LoadShared4<kOffset>(a);
+  const float2 q = LoadShared2<kOffset + 16>(a);
+  return F3{fmaf(w, p.w, p.x), fmaf(w, q.x, p.y), fmaf(w, q.y, p.z)};
+}
+__host__ __device__ constexpr uint32_t RowAdjust(uint32_t base, int stride) {
+  return base - kRoundMagicBits * (uint32_t)stride;
 }
 
-// The staged radiance at nu1 of theta row l: L[n0] + w D[n0].
-__device__ __forceinline__ F3 NuLerp(const float4* __restrict__ P, const float2* __restrict__ Q,
-                                     float nu1, float half_nu, float top, int nmax) {
-  const float u = clampf(fmaf(nu1, half_nu, half_nu), 0.0f, top);
-  const int n0 = min((int)u, nmax);
-  const float w = u - float(n0);
-  const float4 p = P[n0];
-  const float2 q = Q[n0];
-  return F3{fmaf(w, p.w, p.x), fmaf(w, q.x, p.y), fmaf(w, q.y, p.z)};
+// Shared memory of one block, bytes: [16][NU] node entries (the previous
+// order interpolated in mu at the slab's r and mu_s; at order 2 a Rayleigh
+// and a Mie entry per node), the bottom row of the irradiance LUT as [IW]
+// entries, and a float4 staging value per node.
+int DensityFastSmem(const Shape& s, int order) {
+  const int species = order == 2 ? 2 : 1;
+  const int nodes = kDensityThetaSamples * s.snu;
+  return nodes * species * kNodeBytes + s.iw * kNodeBytes +
+         (species * nodes + s.iw) * (int)sizeof(float4);
+}
+
+// Texels of one mu row that a thread integrates together: they share the
+// outgoing direction's phase functions.
+constexpr int kDensityTexelsPerTask = 2;
+
+struct DensityTask {
+  float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];   // sx, sy x sin(theta_l)
+  F3 sum_r[kDensityTexelsPerTask];   // sums of L (1 + nu2^2) dw
+  F3 sum_m[kDensityTexelsPerTask];   // sums of L P_M(nu2) / mie_k dw
+};
+
+// The 32 phi samples of theta row l for the texels of one task.
+template <bool kOrder2, bool kGround>
+__device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts& c, float A,
+                                                float B, float oxs, float dw, float half_nu,
+                                                float nu_off, uint32_t row_adj, F3 tg,
+                                                float g_scale, float g_off, float ir_top,
+                                                uint32_t ir_adj) {
+  constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
+  const float m2g = c.m2g, g2p1 = c.g2p1, ray_k = c.ray_k, mie_k = c.mie_k;
+  // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
+  // the outgoing direction; nu1 differs by the sign of sy sin(phi).
+#pragma unroll 2
+  for (int m = 0; m < kDensityPhiSamples / 2; ++m) {
+    const float2 cs = c_density_phi[m];
+    // Phase functions at nu2 (functions.glsl:739-747, :1245-1254), x dw.
+    const float nu2 = fmaf(oxs, cs.x, B);
+    const float pr = fmaf(nu2, nu2, 1.0f) * dw;
+    const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
+    const float pm = pr * (rs * rs * rs);
+#pragma unroll
+    for (int q = 0; q < kDensityTexelsPerTask; ++q) {
+      const float base = fmaf(task.sxs[q], cs.x, A);   // nu1 = base +- dl
+      const float dl = task.sys[q] * cs.y;
+      const float bu = fmaf(base, half_nu, nu_off);
+      const float bg = kGround ? fmaf(base, g_scale, g_off) : 0.0f;
+      F3 Ls = f3(0.0f);
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const float sdl = side == 0 ? dl : -dl;
+        const float u = fmaxf(fmaf(sdl, half_nu, bu), -0.5f);
+        const float t = u + kRoundMagic;
+        F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
+        if (kOrder2) {
+          // Single scattering with its phase functions at nu1 (:998-1004).
+          const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
+          const float nu1 = base + sdl;
+          const float q1 = fmaf(nu1, nu1, 1.0f);
+          const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
+          L = L * (ray_k * q1) + M * (mie_k * q1 * (r1 * r1 * r1));
+        }
+        if (kGround) {
+          // Ground bounce: the ground point is at radius Rb, so the cosine
+          // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
+          // irradiance lookup at r = Rb reads row 0 of the LUT.
+          const float x = clampf(fmaf(sdl, g_scale, bg), -0.5f, ir_top);
+          L = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), L);
+        }
+        Ls += L;
+      }
+      task.sum_r[q] = fma3(Ls, pr, task.sum_r[q]);
+      task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
+    }
+  }
 }
 
 template <bool kOrder2>
 __global__ void __launch_bounds__(kDensityFastThreads)
 k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   extern __shared__ float4 smem[];
+  constexpr int kSpecies = kOrder2 ? 2 : 1;
+  constexpr int kStride = kSpecies * kNodeBytes;
   int local;
   const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
   const Shape s = in.s;
   const int NU = s.snu, W = s.sw();
   const int k = local / s.smus, col = local % s.smus;
-  const int rows_nu = kDensityThetaSamples * NU;
-  float4* PR = smem;                                          // Rayleigh / multiple
-  float2* QR = reinterpret_cast<float2*>(PR + rows_nu);
-  float4* PM = reinterpret_cast<float4*>(QR + rows_nu);        // Mie (order 2)
-  float2* QM = reinterpret_cast<float2*>(PM + rows_nu);
-  float4* IR = kOrder2 ? reinterpret_cast<float4*>(QM + rows_nu) : PM;   // [iw]
+  const int nodes = kDensityThetaSamples * NU;
+  float4* E = smem;                                            // [nodes][species] entries
+  float4* G = E + nodes * kSpecies * (kNodeBytes / 16);        // [iw] irradiance entries
+  float4* V = G + s.iw * (kNodeBytes / 16);                    // staging values
   const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
 
-  // Stage the previous order, bilinear in mu, at column (n * MU_S + col) of
-  // slice k: first the values, then (after a barrier) the slopes.
-  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
-    const int l = e / NU, n = e % NU;
-    const float Y = drows[l].u_mu * float(s.smu) - 0.5f;
-    const float fy = floorf(Y);
-    const float wy = Y - fy;
-    const int y0 = ClampIdx((int)fy, s.smu), y1 = ClampIdx((int)fy + 1, s.smu);
-    const int base = k * s.smu * W + n * s.smus + col;
-    const float4 a = __ldg(in.dR + base + y0 * W);
-    const float4 b = __ldg(in.dR + base + y1 * W);
-    PR[e] = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
-                        fmaf(wy, b.z - a.z, a.z), 0.0f);
-    if (kOrder2) {
-      const float4 p = __ldg(in.dM + base + y0 * W);
-      const float4 q = __ldg(in.dM + base + y1 * W);
-      PM[e] = make_float4(fmaf(wy, q.x - p.x, p.x), fmaf(wy, q.y - p.y, p.y),
-                          fmaf(wy, q.z - p.z, p.z), 0.0f);
+  // Node values: the previous order (Rayleigh or multiple, then Mie at order
+  // 2) at column n MU_S + col of slice k, bilinear in mu; then the irradiance.
+  const int staged = kSpecies * nodes + s.iw;
+  for (int e = threadIdx.x; e < staged; e += blockDim.x) {
+    float4 v;
+    if (e < kSpecies * nodes) {
+      const int sp = e / nodes, ne = e - sp * nodes;
+      const int l = ne / NU, n = ne - l * NU;
+      const float Y = drows[l].u_mu * float(s.smu) - 0.5f;
+      const float fy = floorf(Y);
+      const float wy = Y - fy;
+      const int y0 = ClampIdx((int)fy, s.smu), y1 = ClampIdx((int)fy + 1, s.smu);
+      const float4* src =
+          (kOrder2 && sp == 1 ? in.dM : in.dR) + k * s.smu * W + n * s.smus + col;
+      const float4 a = __ldg(src + y0 * W), b = __ldg(src + y1 * W);
+      v = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
+                      fmaf(wy, b.z - a.z, a.z), 0.0f);
+    } else {
+      v = __ldg(in.dI + (e - kSpecies * nodes));
     }
-  }
-  for (int e = threadIdx.x; e < s.iw; e += blockDim.x) IR[e] = __ldg(in.dI + e);
-  __syncthreads();
-  // Slopes towards the next node (0 at the last node): y, z into Q, x into a
-  // temporary, then x into P.w once every value has been read.
-  float* TX = reinterpret_cast<float*>(IR + s.iw);                 // [species][rows_nu]
-  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
-    const bool last = (e % NU) == NU - 1;
-    const float4 v = PR[e], nx = last ? v : PR[e + 1];
-    QR[e] = make_float2(nx.y - v.y, nx.z - v.z);
-    TX[e] = nx.x - v.x;
-    if (kOrder2) {
-      const float4 vm = PM[e], nm = last ? vm : PM[e + 1];
-      QM[e] = make_float2(nm.y - vm.y, nm.z - vm.z);
-      TX[rows_nu + e] = nm.x - vm.x;
-    }
+    V[e] = v;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < rows_nu; e += blockDim.x) {
-    PR[e].w = TX[e];
-    if (kOrder2) PM[e].w = TX[rows_nu + e];
+  for (int e = threadIdx.x; e < staged; e += blockDim.x) {
+    if (e < kSpecies * nodes) {
+      const int sp = e / nodes, ne = e - sp * nodes;
+      const bool last = (ne % NU) == NU - 1;
+      StoreNode(E + (ne * kSpecies + sp) * (kNodeBytes / 16), V[e], last ? V[e] : V[e + 1]);
+    } else {
+      const int i = e - kSpecies * nodes;
+      StoreNode(G + i * (kNodeBytes / 16), V[e], i == s.iw - 1 ? V[e] : V[e + 1]);
+    }
   }
   __syncthreads();
 
   const Consts& c = in.c;
-  const float m2g = c.m2g, g2p1 = c.g2p1, ray_k = c.ray_k, mie_k = c.mie_k;
   const TexelCol cc = in.tab.cols[col];
   const float half_nu = 0.5f * float(NU - 1);
-  const float top = float(NU - 1);
-  const int nmax = NU - 2;
+  const float nu_off = half_nu - 0.5f;
   const float iw1 = float(s.iw - 1);
-  const int imax = s.iw - 2;
-  const float inv_rb = 1.0f / c.Rb;
+  const float ir_top = float(s.iw) - 1.5f;
+  const float half_inv_rb = 0.5f / c.Rb;
   const float dtdp = (kPiF / 16.0f) * (kPiF / 16.0f);
-  const int texels = NU * s.smu;
-  for (int t = threadIdx.x; t < texels; t += blockDim.x) {
-    const int j = t % s.smu, n = t / s.smu;
+  const uint32_t e_base = (uint32_t)__cvta_generic_to_shared(E);
+  const uint32_t ir_adj = RowAdjust((uint32_t)__cvta_generic_to_shared(G), kNodeBytes);
+  const int per_row = (NU + kDensityTexelsPerTask - 1) / kDensityTexelsPerTask;
+  const int tasks = s.smu * per_row;
+  for (int ti = threadIdx.x; ti < tasks; ti += blockDim.x) {
+    const int j = ti % s.smu, n0 = (ti / s.smu) * kDensityTexelsPerTask;
     const TexelRow row = in.tab.rows[k * s.smu + j];
-    const TexelAngles ang = MakeAngles(s, row, cc, n);
-    const float rmu_s = row.r * ang.mu_s;
-    F3 sum_r = f3(0.0f), sum_m = f3(0.0f);   // sums of L (1 + nu2^2) and L P_M(nu2) / mie_k
+    float sx[kDensityTexelsPerTask], sy[kDensityTexelsPerTask];
+    DensityTask task;
+#pragma unroll
+    for (int q = 0; q < kDensityTexelsPerTask; ++q) {
+      const TexelAngles ang = MakeAngles(s, row, cc, min(n0 + q, NU - 1));
+      sx[q] = ang.sx;
+      sy[q] = ang.sy;
+      task.sum_r[q] = f3(0.0f);
+      task.sum_m[q] = f3(0.0f);
+    }
+    // Irradiance texel coordinate - 0.5 of the ground point at nu1 = 0:
+    // (mu_g / 2 + 1 / 2) (IW - 1) with mu_g = (r mu_s + dist nu1) / Rb.
+    const float g_off = fmaf(fmaf(row.r * cc.mu_s, half_inv_rb, 0.5f), iw1, -0.5f);
     for (int l = 0; l < kDensityThetaSamples; ++l) {
       const DensityRow dr = drows[l];
-      const float A = ang.mu_s * dr.cos_t, B = ang.mu * dr.cos_t;
-      const float sxs = ang.sx * dr.sin_t, sys = ang.sy * dr.sin_t;
-      const float oxs = ang.omega_x * dr.sin_t;
-      const float4* Pr = PR + l * NU;
-      const float2* Qr = QR + l * NU;
-      const float4* Pm = PM + l * NU;
-      const float2* Qm = QM + l * NU;
-      const F3 tg = f3(dr.t_ground);
-      const bool ground = dr.ground != 0;
-      F3 row_r = f3(0.0f), row_m = f3(0.0f);
-      // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions
-      // of the outgoing direction; nu1 differs by the sign of sy sin(phi).
-#pragma unroll 2
-      for (int m = 0; m < kDensityPhiSamples / 2; ++m) {
-        const float2 cs = c_density_phi[m];
-        const float base = fmaf(sxs, cs.x, A);
-        const float dl = sys * cs.y;
-        const float nu2 = fmaf(oxs, cs.x, B);
-        F3 Ls = f3(0.0f);
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-          const float nu1 = side == 0 ? base + dl : base - dl;
-          F3 L = NuLerp(Pr, Qr, nu1, half_nu, top, nmax);
-          if (kOrder2) {
-            // Single scattering with its phase functions at nu1 (:998-1004).
-            const F3 M = NuLerp(Pm, Qm, nu1, half_nu, top, nmax);
-            const float q1 = fmaf(nu1, nu1, 1.0f);
-            const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
-            L = L * (ray_k * q1) + M * (mie_k * q1 * (r1 * r1 * r1));
-          }
-          if (ground) {
-            // Ground bounce: the ground point is at radius Rb, so the cosine
-            // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
-            // irradiance lookup at r = Rb reads row 0 of the LUT.
-            const float mu_g = fmaf(dr.dist_ground, nu1, rmu_s) * inv_rb;
-            const float X = clampf(fmaf(mu_g, 0.5f, 0.5f), 0.0f, 1.0f) * iw1;
-            const int i0 = min((int)X, imax);
-            const float wi = X - float(i0);
-            const float4 e0 = IR[i0], e1 = IR[i0 + 1];
-            L = fma3(tg, F3{fmaf(wi, e1.x - e0.x, e0.x), fmaf(wi, e1.y - e0.y, e0.y),
-                            fmaf(wi, e1.z - e0.z, e0.z)}, L);
-          }
-          Ls += L;
-        }
-        // Phase functions at nu2 (functions.glsl:739-747, :1245-1254).
-        const float q = fmaf(nu2, nu2, 1.0f);
-        const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
-        row_r = fma3(Ls, q, row_r);
-        row_m = fma3(Ls, q * (rs * rs * rs), row_m);
-      }
+      const float A = cc.mu_s * dr.cos_t, B = row.mu * dr.cos_t;
+      const float oxs = row.omega_x * dr.sin_t;
       const float dw = dtdp * dr.sin_t;
-      sum_r = fma3(row_r, dw, sum_r);
-      sum_m = fma3(row_m, dw, sum_m);
+#pragma unroll
+      for (int q = 0; q < kDensityTexelsPerTask; ++q) {
+        task.sxs[q] = sx[q] * dr.sin_t;
+        task.sys[q] = sy[q] * dr.sin_t;
+      }
+      const uint32_t row_adj = RowAdjust(e_base + (uint32_t)(l * NU * kStride), kStride);
+      if (dr.ground) {
+        DensityThetaRow<kOrder2, true>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
+                                       f3(dr.t_ground), dr.dist_ground * half_inv_rb * iw1,
+                                       g_off, ir_top, ir_adj);
+      } else {
+        DensityThetaRow<kOrder2, false>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
+                                        f3(0.0f), 0.0f, 0.0f, 0.0f, ir_adj);
+      }
     }
-    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * ray_k);
-    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * mie_k);
-    const F3 J = a_r * sum_r + a_m * sum_m;
-    const int texel = (k * s.smu + j) * W + n * s.smus + col;
-    in.dJ[texel] = to4(J, 1.0f);
+    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
+    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+#pragma unroll
+    for (int q = 0; q < kDensityTexelsPerTask; ++q) {
+      if (n0 + q < NU) {
+        const F3 J = a_r * task.sum_r[q] + a_m * task.sum_m[q];
+        in.dJ[(k * s.smu + j) * W + (n0 + q) * s.smus + col] = to4(J, 1.0f);
+      }
+    }
   }
 }
 
