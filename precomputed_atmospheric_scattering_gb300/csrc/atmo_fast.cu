@@ -493,6 +493,210 @@ cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, in
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Single scattering, restructured (functions.glsl:650-730, :933-945).
+//
+// As for multiple scattering, a sample's r, altitude, densities and the
+// transmittance from the texel to it depend on the texel's row only; the
+// transmittance from the sample to the sun depends on mu_s at the sample,
+// hence on the texel's column.  Its LUT lookup happens at the sample's
+// (rho, r): a fixed pair of transmittance LUT rows.  Per sample the block
+// interpolates those two rows into a line of W_T columns in shared memory; a
+// texel computes the x_mu of its sun direction and reads 2 line entries.
+// ---------------------------------------------------------------------------
+constexpr int kSingleSamples = kSingleScatteringSamples + 1;
+
+struct __align__(16) SunSample {
+  int t0, t1;                // element offsets of the transmittance LUT rows j0, j1
+  float b;                   // weight of row j1
+  float rho, r, inv_r;       // the sample's rho, r and 1 / r
+  float e_sun;               // sin(theta_h) alpha_s = Rb / r alpha_s
+  float d;                   // distance from the texel's point along its ray
+  float dens_r, dens_m;      // Rayleigh and Mie densities x trapezoid weight
+  float tx, ty, tz;          // transmittance texel -> sample
+  float inv_range;           // 1 / (d_max - d_min) of the transmittance mapping
+  float pad[2];
+};
+
+__host__ __device__ inline MultipleFastDims SingleDims(const Shape& s) {
+  int rows = kMultipleFastThreads / s.sw();
+  rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
+  int group = 32768 / (2 * 16 * rows * s.tw);
+  group = group < 1 ? 1 : (group > 4 ? 4 : group);
+  return MultipleFastDims{rows, group};
+}
+int SingleFastSmem(const Shape& s) {
+  const MultipleFastDims d = SingleDims(s);
+  return d.rows * kSingleSamples * (int)sizeof(SunSample) + 2 * d.group * d.rows * s.tw * 16;
+}
+bool SingleFastFits(const Shape& s) {
+  return s.sw() <= kMultipleFastThreads * kMultipleFastMaxCols && SingleFastSmem(s) <= 48 * 1024;
+}
+int SingleFastTiles(const Shape& s) {
+  const int rows = SingleDims(s).rows;
+  return (s.sr * s.smu + rows - 1) / rows;
+}
+
+// Sample i of the ray of LUT row `rowi` (the per-sample part of
+// SingleScatteringTexel that does not depend on mu_s or nu).
+__device__ SunSample MakeSunSample(const Instance& in, int rowi, int i) {
+  const Consts& c = in.c;
+  const Shape& s = in.s;
+  const TexelRow row = in.tab.rows[rowi];
+  const bool ground = row.ground != 0;
+  const float dx = row.d / float(kSingleScatteringSamples);
+  const float d = float(i) * dx;
+  const float e = float(kSingleScatteringSamples - i) * dx;
+  const RadialPoint p = PointFromRho2(c, RayRho2(row, d, e));
+  const TStart start = MakeTStart(c, s, in.T, in.Tau, row.rho, row.r,
+                                  ground ? -row.rmu : row.rmu, row.delta);
+  const F3 t = SegmentTransmittance(c, s, in.T, in.Tau, row.rmu, row.delta, p, d, ground, start);
+  const float w = (i == 0 || i == kSingleScatteringSamples) ? 0.5f : 1.0f;
+  const float Y = p.rho / c.H * float(s.th - 1);
+  const float fy = floorf(Y);
+  const int j0 = ClampIdx((int)fy, s.th), j1 = ClampIdx((int)fy + 1, s.th);
+  SunSample ss;
+  ss.t0 = j0 * s.tw;
+  ss.t1 = j1 * s.tw;
+  ss.b = Y - fy;
+  ss.rho = p.rho;
+  ss.r = p.r;
+  ss.inv_r = 1.0f / p.r;
+  ss.e_sun = c.Rb / p.r * c.alpha_s;
+  ss.d = d;
+  ss.dens_r = ProfileDensity(c.prof_r, p.h) * w;
+  ss.dens_m = ProfileDensity(c.prof_m, p.h) * w;
+  ss.tx = t.x;
+  ss.ty = t.y;
+  ss.tz = t.z;
+  const float d_min = (c.H - p.rho) * (c.H + p.rho) / (c.Rt + p.r);
+  ss.inv_range = 1.0f / (p.rho + c.H - d_min);
+  ss.pad[0] = ss.pad[1] = 0.0f;
+  return ss;
+}
+
+template <int kCols>
+__device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, float4* smem) {
+  const Shape s = in.s;
+  const Consts& c = in.c;
+  const MultipleFastDims dims = SingleDims(s);
+  const int W = s.sw(), R = dims.rows, G = dims.group, TW = s.tw;
+  const int rows_total = s.sr * s.smu;
+  const int row0 = local * R;
+  SunSample* samp = reinterpret_cast<SunSample*>(smem);                       // [R][51]
+  float4* line = smem + R * kSingleSamples * (int)(sizeof(SunSample) / 16);   // [2][G][R][TW]
+
+  for (int e = threadIdx.x; e < R * kSingleSamples; e += kMultipleFastThreads) {
+    const int rr = e / kSingleSamples, i = e - rr * kSingleSamples;
+    if (row0 + rr < rows_total) samp[e] = MakeSunSample(in, row0 + rr, i);
+  }
+
+  const int rr = kCols == 1 ? (int)threadIdx.x / W : 0;
+  const int x_t = kCols == 1 ? (int)threadIdx.x - rr * W : (int)threadIdx.x;
+  const int rowi = row0 + rr;
+  const bool active = rr < R && rowi < rows_total;
+  const int nmax = W - 1;
+  float rmu_s[kCols], nu[kCols];
+  F3 sum_r[kCols], sum_m[kCols];
+  if (active) {
+    const TexelRow row = in.tab.rows[rowi];
+#pragma unroll
+    for (int m = 0; m < kCols; ++m) {
+      const int x = min(x_t + m * kMultipleFastThreads, nmax);
+      const int n = x / s.smus, col = x - n * s.smus;
+      const TexelAngles ang = MakeAngles(s, row, in.tab.cols[col], n);
+      rmu_s[m] = row.r * ang.mu_s;
+      nu[m] = ang.nu;
+      sum_r[m] = f3(0.0f);
+      sum_m[m] = f3(0.0f);
+    }
+  }
+  __syncthreads();
+
+  const float H = c.H, H2 = c.H * c.H;
+  const float tw1 = float(TW - 1);
+  const int line_stride = G * R * TW;
+  const int stages = (kSingleSamples + G - 1) / G;
+  for (int stage = 0; stage < stages; ++stage) {
+    float4* buf = line + (stage & 1) * line_stride;
+    const int first = stage * G;
+    const int count = min(G, kSingleSamples - first);
+    // Transmittance LUT rows j0, j1 of each sample, interpolated in rho.
+    for (int g = 0; g < count; ++g) {
+      for (int q = 0; q < R; ++q) {
+        if (row0 + q >= rows_total) break;
+        const SunSample& sm = samp[q * kSingleSamples + first + g];
+        float4* out = buf + (g * R + q) * TW;
+        for (int x = threadIdx.x; x < TW; x += kMultipleFastThreads) {
+          const float4 a = __ldg(in.T + sm.t0 + x), b = __ldg(in.T + sm.t1 + x);
+          out[x] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
+                               fmaf(sm.b, b.z - a.z, a.z), 0.0f);
+        }
+      }
+    }
+    __syncthreads();
+    if (active) {
+      for (int g = 0; g < count; ++g) {
+        const SunSample& sm = samp[rr * kSingleSamples + first + g];
+        const float4* L = buf + (g * R + rr) * TW;
+#pragma unroll
+        for (int m = 0; m < kCols; ++m) {
+          if (kCols > 1 && x_t + m * kMultipleFastThreads >= W) break;
+          // GetTransmittanceToSun (functions.glsl:552-563) at the sample, with
+          // the lookup mapping of TransmittanceCoords.
+          const float rmu = clampf(fmaf(sm.d, nu[m], rmu_s[m]), -sm.r, sm.r);
+          const float sun = smoothstepf(-sm.e_sun, sm.e_sun, (rmu + sm.rho) * sm.inv_r);
+          const float delta = (sm.rho - rmu) * (sm.rho + rmu);
+          const float sq = sqrtf(fmaxf(H2 - delta, 0.0f));
+          const float rho_minus_a =
+              rmu < 0.0f ? (sm.rho - rmu > 0.0f ? delta / (sm.rho - rmu) : 0.0f) : sm.rho + rmu;
+          const float omx = clampf((rho_minus_a + delta / (H + sq)) * sm.inv_range, 0.0f, 1.0f);
+          const float Xc = omx * tw1;
+          const float f = floorf(Xc);
+          const float gw = Xc - f;   // weight of the lower column
+          const int i_hi = TW - 1 - (int)f;
+          const int i_lo = max(i_hi - 1, 0);
+          const float4 lo = L[i_lo], hi = L[max(i_hi, 0)];
+          const F3 tsun{fmaf(gw, lo.x - hi.x, hi.x), fmaf(gw, lo.y - hi.y, hi.y),
+                        fmaf(gw, lo.z - hi.z, hi.z)};
+          const F3 t = F3{sm.tx, sm.ty, sm.tz} * (tsun * sun);
+          sum_r[m] = fma3(t, sm.dens_r, sum_r[m]);
+          sum_m[m] = fma3(t, sm.dens_m, sum_m[m]);
+        }
+      }
+    }
+  }
+
+  if (!active) return;
+  const float dx = in.tab.rows[rowi].d / float(kSingleScatteringSamples);
+#pragma unroll
+  for (int m = 0; m < kCols; ++m) {
+    const int x = x_t + m * kMultipleFastThreads;
+    if (kCols > 1 && x >= W) break;
+    StoreSingleScattering(in, (long long)rowi * W + x, sum_r[m] * dx * c.solar * c.rayleigh,
+                          sum_m[m] * dx * c.solar * c.mie_sca);
+  }
+}
+
+__global__ void __launch_bounds__(kMultipleFastThreads)
+k_single_fast(const Instance* __restrict__ insts, WorkList wl) {
+  extern __shared__ float4 smem[];
+  int local;
+  const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
+  if (in.s.sw() <= kMultipleFastThreads) {
+    SingleFastBlock<1>(in, local, smem);
+  } else {
+    SingleFastBlock<kMultipleFastMaxCols>(in, local, smem);
+  }
+}
+
+cudaError_t LaunchSingleFast(const Instance* insts, WorkList wl, int tiles, int smem_bytes,
+                             cudaStream_t st) {
+  // smem_bytes: the largest SingleFastSmem of the work list's instances.
+  k_single_fast<<<tiles, kMultipleFastThreads, (size_t)smem_bytes, st>>>(insts, wl);
+  return cudaGetLastError();
+}
+
 __global__ void k_to_half(const float4* __restrict__ src, __half2* __restrict__ dst, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;

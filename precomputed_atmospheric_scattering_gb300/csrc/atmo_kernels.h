@@ -26,6 +26,13 @@ int DensityFastTiles(const Shape& s);
 int DensityFastSmem(const Shape& s, int order);
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
                               int smem_bytes, cudaStream_t st);
+// The row-restructured single-scattering kernel needs W = NU x MU_S <= 1024
+// and its transmittance lines within 48 KB of shared memory.
+bool SingleFastFits(const Shape& s);
+int SingleFastTiles(const Shape& s);
+int SingleFastSmem(const Shape& s);
+cudaError_t LaunchSingleFast(const Instance* insts, WorkList wl, int tiles, int smem_bytes,
+                             cudaStream_t st);
 // The row-restructured multiple-scattering kernel needs W = NU x MU_S <= 1024.
 bool MultipleFastFits(const Shape& s);
 int MultipleFastTiles(const Shape& s);

@@ -88,8 +88,9 @@ size_t Storage::Bytes() const {
 // Program
 // ---------------------------------------------------------------------------
 atmo_path PassPath(Pass pass, const Shape& s, atmo_path path) {
-  if (pass == Pass::kMultiple && path == ATMO_PATH_FAST && !MultipleFastFits(s))
-    return ATMO_PATH_PLAIN;
+  if (path != ATMO_PATH_FAST) return path;
+  if (pass == Pass::kMultiple && !MultipleFastFits(s)) return ATMO_PATH_PLAIN;
+  if (pass == Pass::kSingle && !SingleFastFits(s)) return ATMO_PATH_PLAIN;
   return path;
 }
 
@@ -97,6 +98,7 @@ int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path) {
   if (path != ATMO_PATH_FAST) return 0;
   if (pass == Pass::kDensity) return DensityFastSmem(s, order);
   if (pass == Pass::kMultiple) return MultipleFastSmem(s);
+  if (pass == Pass::kSingle) return SingleFastSmem(s);
   return 0;
 }
 
@@ -106,7 +108,8 @@ int Tiles(Pass pass, const Shape& s, atmo_path path) {
     case Pass::kTables: return TableTiles(s);
     case Pass::kTransmittance: return cdiv(s.t_texels(), kTransmittanceTexelsPerTile);
     case Pass::kDirect: return cdiv(s.i_texels() + s.sr * kDensityThetaSamples, kTexelThreads);
-    case Pass::kSingle: return cdiv(s.s_texels(), kTexelThreads);
+    case Pass::kSingle:
+      return path == ATMO_PATH_FAST ? SingleFastTiles(s) : cdiv(s.s_texels(), kTexelThreads);
     case Pass::kDensity:
       return path == ATMO_PATH_FAST ? DensityFastTiles(s) : cdiv(s.s_texels(), kTexelThreads);
     case Pass::kIndirect: return cdiv(s.i_texels(), kIndirectTexelsPerTile);
@@ -264,7 +267,9 @@ cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, Wo
     case Pass::kTables: return LaunchTables(insts, wl, tiles, st);
     case Pass::kTransmittance: return LaunchTransmittance(insts, wl, tiles, st);
     case Pass::kDirect: return LaunchDirectIrradiance(insts, wl, tiles, st);
-    case Pass::kSingle: return LaunchSingleScattering(insts, wl, tiles, st);
+    case Pass::kSingle:
+      return path == ATMO_PATH_FAST ? LaunchSingleFast(insts, wl, tiles, smem, st)
+                                    : LaunchSingleScattering(insts, wl, tiles, st);
     case Pass::kDensity:
       return path == ATMO_PATH_FAST ? LaunchDensityFast(insts, wl, tiles, order, smem, st)
                                     : LaunchDensityPlain(insts, wl, tiles, order, st);

@@ -93,8 +93,8 @@ class Program {
 };
 
 // The kernel variant that runs `pass` for shape s when `path` is requested:
-// the fast multiple-scattering kernel holds a LUT row of NU x MU_S texels in
-// shared memory and takes shapes up to 1024 of them.
+// the fast single- and multiple-scattering kernels hold a LUT row of NU x MU_S
+// texels per block and take shapes up to 1024 of them.
 atmo_path PassPath(Pass pass, const Shape& s, atmo_path path);
 // Blocks and dynamic shared memory of `pass` for shape s under the variant
 // `path` (as PassPath returns it).
