@@ -104,7 +104,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
                                                 float g_scale, float g_off, float ir_top,
                                                 uint32_t ir_adj) {
   constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
-  const float m2g = c.m2g, g2p1 = c.g2p1, ray_k = c.ray_k, mie_k = c.mie_k;
+  const float m2g = c.m2g, g2p1 = c.g2p1;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
   // the outgoing direction; nu1 differs by the sign of sy sin(phi).
 #pragma unroll 2
@@ -127,23 +127,25 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
         const float sdl = side == 0 ? dl : -dl;
         const float u = fmaxf(fmaf(sdl, half_nu, bu), -0.5f);
         const float t = u + kRoundMagic;
-        F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
+        const F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
         if (kOrder2) {
-          // Single scattering with its phase functions at nu1 (:998-1004).
+          // Single scattering with its phase functions at nu1 (:998-1004):
+          // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
+          // with the constant factors staged into the tables.
           const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
           const float nu1 = base + sdl;
-          const float q1 = fmaf(nu1, nu1, 1.0f);
           const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
-          L = L * (ray_k * q1) + M * (mie_k * q1 * (r1 * r1 * r1));
+          Ls = fma3(fma3(M, r1 * r1 * r1, L), fmaf(nu1, nu1, 1.0f), Ls);
+        } else {
+          Ls += L;
         }
         if (kGround) {
           // Ground bounce: the ground point is at radius Rb, so the cosine
           // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
           // irradiance lookup at r = Rb reads row 0 of the LUT.
           const float x = clampf(fmaf(sdl, g_scale, bg), -0.5f, ir_top);
-          L = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), L);
+          Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), Ls);
         }
-        Ls += L;
       }
       task.sum_r[q] = fma3(Ls, pr, task.sum_r[q]);
       task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
@@ -183,8 +185,10 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
       const float4* src =
           (kOrder2 && sp == 1 ? in.dM : in.dR) + k * s.smu * W + n * s.smus + col;
       const float4 a = __ldg(src + y0 * W), b = __ldg(src + y1 * W);
-      v = make_float4(fmaf(wy, b.x - a.x, a.x), fmaf(wy, b.y - a.y, a.y),
-                      fmaf(wy, b.z - a.z, a.z), 0.0f);
+      // At order 2 the single-scattering tables carry their phase constants.
+      const float scale = kOrder2 ? (sp == 1 ? in.c.mie_k : in.c.ray_k) : 1.0f;
+      v = make_float4(fmaf(wy, b.x - a.x, a.x) * scale, fmaf(wy, b.y - a.y, a.y) * scale,
+                      fmaf(wy, b.z - a.z, a.z) * scale, 0.0f);
     } else {
       v = __ldg(in.dI + (e - kSpecies * nodes));
     }
@@ -368,6 +372,19 @@ __device__ RaySample MakeRaySample(const Instance& in, int rowi, int i) {
   return rs;
 }
 
+// UMuSFromMuS with the mapping's constant divisions replaced by products
+// (inv_range = 1 / (d_max - d_min), inv_A = 1 / A) and the others approximate
+// (<= 2 ulp): for samples along a ray, whose mu_s is not a texel's own.
+__device__ __forceinline__ float UMuSFromMuSAlongRay(const Consts& c, const Shape& s, float mu_s,
+                                                     float inv_range, float inv_A) {
+  const float H2 = c.H * c.H;
+  const float rmus = c.Rb * mu_s;
+  const float sq = sqrtf(fmaf(rmus, rmus, H2));
+  const float d = rmus > 0.0f ? __fdividef(H2, rmus + sq) : sq - rmus;
+  const float a = (d - (c.Rt - c.Rb)) * inv_range;
+  return TexCoord(s, kMapSMUS, __fdividef(fmaxf(fmaf(-a, inv_A, 1.0f), 0.0f), 1.0f + a));
+}
+
 template <int kCols>
 __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local, float4* smem) {
   const Shape s = in.s;
@@ -391,6 +408,8 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
   const bool active = rr < R && rowi < rows_total;
   const float smus_f = float(s.smus);
   const int nmax = W - 1;
+  const float inv_range = 1.0f / (c.H - (c.Rt - c.Rb));
+  const float inv_A = 1.0f / c.mus_A;
   float rmu_s[kCols], nu[kCols], xb[kCols], lnu[kCols];
   F3 acc[kCols];
   if (active) {
@@ -443,7 +462,8 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
         for (int m = 0; m < kCols; ++m) {
           if (kCols > 1 && x_t + m * kMultipleFastThreads >= W) break;
           const float mu_s_i = clampf(fmaf(sm.d, nu[m], rmu_s[m]) * sm.inv_r, -1.0f, 1.0f);
-          const float x0 = fmaf(UMuSFromMuS(c, s, mu_s_i), smus_f, xb[m]);
+          const float x0 =
+              fmaf(UMuSFromMuSAlongRay(c, s, mu_s_i, inv_range, inv_A), smus_f, xb[m]);
           const float fx = floorf(x0);
           const float a = x0 - fx;
           const int i0 = (int)fx;
@@ -474,7 +494,7 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
   }
 }
 
-__global__ void __launch_bounds__(kMultipleFastThreads)
+__global__ void __launch_bounds__(kMultipleFastThreads, 4)
 k_multiple_fast(const Instance* __restrict__ insts, WorkList wl) {
   extern __shared__ float4 smem[];
   int local;
@@ -510,7 +530,7 @@ struct __align__(16) SunSample {
   int t0, t1;                // element offsets of the transmittance LUT rows j0, j1
   float b;                   // weight of row j1
   float rho, r, inv_r;       // the sample's rho, r and 1 / r
-  float e_sun;               // sin(theta_h) alpha_s = Rb / r alpha_s
+  float inv_2e;              // 1 / (2 sin(theta_h) alpha_s), sin(theta_h) = Rb / r
   float d;                   // distance from the texel's point along its ray
   float dens_r, dens_m;      // Rayleigh and Mie densities x trapezoid weight
   float tx, ty, tz;          // transmittance texel -> sample
@@ -562,7 +582,8 @@ __device__ SunSample MakeSunSample(const Instance& in, int rowi, int i) {
   ss.rho = p.rho;
   ss.r = p.r;
   ss.inv_r = 1.0f / p.r;
-  ss.e_sun = c.Rb / p.r * c.alpha_s;
+  // 1 / 0 = +inf for a point sun: the smoothstep then becomes a step at 0.
+  ss.inv_2e = 1.0f / (2.0f * (c.Rb / p.r * c.alpha_s));
   ss.d = d;
   ss.dens_r = ProfileDensity(c.prof_r, p.h) * w;
   ss.dens_m = ProfileDensity(c.prof_m, p.h) * w;
@@ -645,12 +666,16 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
           // GetTransmittanceToSun (functions.glsl:552-563) at the sample, with
           // the lookup mapping of TransmittanceCoords.
           const float rmu = clampf(fmaf(sm.d, nu[m], rmu_s[m]), -sm.r, sm.r);
-          const float sun = smoothstepf(-sm.e_sun, sm.e_sun, (rmu + sm.rho) * sm.inv_r);
+          // smoothstep(-e, e, mu_s - cos(theta_h)), cos(theta_h) = -rho / r.
+          const float st = clampf((rmu + sm.rho) * sm.inv_r * sm.inv_2e + 0.5f, 0.0f, 1.0f);
+          const float sun = st * st * fmaf(-2.0f, st, 3.0f);
           const float delta = (sm.rho - rmu) * (sm.rho + rmu);
           const float sq = sqrtf(fmaxf(H2 - delta, 0.0f));
           const float rho_minus_a =
-              rmu < 0.0f ? (sm.rho - rmu > 0.0f ? delta / (sm.rho - rmu) : 0.0f) : sm.rho + rmu;
-          const float omx = clampf((rho_minus_a + delta / (H + sq)) * sm.inv_range, 0.0f, 1.0f);
+              rmu < 0.0f ? (sm.rho - rmu > 0.0f ? __fdividef(delta, sm.rho - rmu) : 0.0f)
+                         : sm.rho + rmu;
+          const float omx =
+              clampf((rho_minus_a + __fdividef(delta, H + sq)) * sm.inv_range, 0.0f, 1.0f);
           const float Xc = omx * tw1;
           const float f = floorf(Xc);
           const float gw = Xc - f;   // weight of the lower column
