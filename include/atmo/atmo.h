@@ -19,6 +19,12 @@
  *   texture sizes              atmosphere/constants.h:47-61 atmo_lut_shape
  *   glGetTexImage read-back    atmosphere/demo/webgl/precompute.cc:63-72
  *                                                          atmo_model_read_lut
+ *   shader API (GLSL)          atmosphere/model.cc:221-281, functions.glsl:1633-1896
+ *     GetSolarRadiance/Luminance                          atmo_solar_radiance
+ *     GetSkyRadiance/Luminance                            atmo_sky_radiance
+ *     GetSkyRadiance/LuminanceToPoint                     atmo_sky_radiance_to_point
+ *     GetSunAndSkyIrradiance/Illuminance                  atmo_sun_and_sky_irradiance
+ *     (a demo-style pinhole view of all three)            atmo_shade_view
  *
  * All entry points return an atmo_status.  Plain C types only: device
  * pointers are exported as integers/void*, streams as opaque pointers that
@@ -146,6 +152,7 @@ typedef enum { ATMO_PATH_FAST = 0, ATMO_PATH_PLAIN = 1 } atmo_path;
 
 typedef struct atmo_model atmo_model;
 typedef struct atmo_batch atmo_batch;
+typedef struct atmo_lut_set atmo_lut_set;
 
 /* ---- library --------------------------------------------------------------- */
 int atmo_abi_version(void);
@@ -261,6 +268,63 @@ atmo_status atmo_batch_kernel_count(const atmo_batch* batch, unsigned* count);
 atmo_status atmo_batch_time_passes(atmo_batch* batch, atmo_stream stream, unsigned capacity,
                                    float* ms, int* pass, int* order, unsigned* count);
 
+/* ---- render-time queries ---------------------------------------------------- */
+/* The shader API of atmosphere/model.cc:221-281 (functions.glsl:1705-1896),
+   evaluated by CUDA kernels on a resident LUT set instead of in a GLSL
+   shader.  A LUT set is the ATMOSPHERE constant plus the textures of one
+   precomputation: a model's after atmo_model_init (the atmosphere at
+   kLambdaR/G/B with the header's 6-decimal rounding; valid until the model is
+   destroyed, refreshed by each Init) or instance i of a batch after
+   atmo_batch_run (refreshed by each run).
+   Query arrays are DEVICE arrays of n float triples in length units, the
+   planet centre at the origin; directions are unit vectors.  sun_direction
+   holds one direction for every query (sun_stride 0) or one per query
+   (sun_stride 3); shadow_length may be NULL (0 for every query).
+   luminance != 0 selects the luminance API (GetSkyLuminance ...: results
+   times SKY_/SUN_SPECTRAL_RADIANCE_TO_LUMINANCE); luminance == 0 the radiance
+   API, which the reference enables only for <= 3 precomputed wavelengths.
+   Batch instances have no spectrum, hence no luminance API.
+   The scattering texture is read in float32 also for half-precision models. */
+atmo_status atmo_model_lut_set(const atmo_model* model, const atmo_lut_set** out);
+atmo_status atmo_batch_lut_set(const atmo_batch* batch, unsigned i, const atmo_lut_set** out);
+/* radiance[n][3], transmittance[n][3] (may be NULL). */
+atmo_status atmo_sky_radiance(const atmo_lut_set* set, const float* camera, const float* view_ray,
+                              const float* shadow_length, const float* sun_direction,
+                              int sun_stride, unsigned n, int luminance, float* radiance,
+                              float* transmittance, atmo_stream stream);
+atmo_status atmo_sky_radiance_to_point(const atmo_lut_set* set, const float* camera,
+                                       const float* point, const float* shadow_length,
+                                       const float* sun_direction, int sun_stride, unsigned n,
+                                       int luminance, float* radiance, float* transmittance,
+                                       atmo_stream stream);
+/* sun_irradiance[n][3] (the return value of GetSunAndSkyIrradiance),
+   sky_irradiance[n][3] (may be NULL). */
+atmo_status atmo_sun_and_sky_irradiance(const atmo_lut_set* set, const float* point,
+                                        const float* normal, const float* sun_direction,
+                                        int sun_stride, unsigned n, int luminance,
+                                        float* sun_irradiance, float* sky_irradiance,
+                                        atmo_stream stream);
+/* GetSolarRadiance / GetSolarLuminance (host). */
+atmo_status atmo_solar_radiance(const atmo_lut_set* set, int luminance, double out[3]);
+/* A pinhole view: pixel (i, j) of width x height (row j from the top) looks
+   along normalize(forward + ((2i+1)/width - 1) tan(fov_y/2) width/height right
+   + (1 - (2j+1)/height) tan(fov_y/2) up). */
+typedef struct {
+  float camera[3];
+  float right[3], up[3], forward[3];
+  float fov_y;                 /* radians */
+  int width, height;
+  float sun_direction[3];
+  float albedo[3];             /* of the shaded points */
+} atmo_pinhole_view;
+/* One shading request over a pinhole view (device arrays, row-major pixels):
+   sky_rgba[pixel] = GetSkyRadiance(camera, view ray) (alpha: the green
+   transmittance); shaded_rgba[pixel] = GetSkyRadianceToPoint(camera, p) +
+   transmittance x albedo / pi x (sun + sky irradiance of GetSunAndSkyIrradiance
+   at p with normal -view ray), p = camera + depth[pixel] x view ray. */
+atmo_status atmo_shade_view(const atmo_lut_set* set, const atmo_pinhole_view* view,
+                            const float* depth, int luminance, float* sky_rgba,
+                            float* shaded_rgba, atmo_stream stream);
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Measures this GPU's FP32 FMA throughput (TFLOP/s, 2 FLOP per FMA) with a
    short dependent-chain kernel over every SM: the denominator of the

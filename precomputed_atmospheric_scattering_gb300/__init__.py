@@ -118,6 +118,16 @@ class Atmosphere(C.Structure):
         return a
 
 
+_F3 = C.c_float * 3
+
+
+class PinholeView(C.Structure):
+    """atmo_pinhole_view: a 1920x1080-style pinhole camera for atmo_shade_view."""
+    _fields_ = [("camera", _F3), ("right", _F3), ("up", _F3), ("forward", _F3),
+                ("fov_y", C.c_float), ("width", C.c_int), ("height", C.c_int),
+                ("sun_direction", _F3), ("albedo", _F3)]
+
+
 class LutView(C.Structure):
     _fields_ = [("device_ptr", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
                 ("depth", C.c_int), ("dtype", C.c_int), ("bytes", C.c_size_t)]
@@ -179,6 +189,15 @@ def lib():
             "atmo_measure_fp32_peak": [P(C.c_double)],
             "atmo_batch_time_passes": [vp, vp, C.c_uint, P(C.c_float), P(C.c_int), P(C.c_int),
                                        P(C.c_uint)],
+            "atmo_model_lut_set": [vp, P(vp)],
+            "atmo_batch_lut_set": [vp, C.c_uint, P(vp)],
+            "atmo_sky_radiance": [vp, vp, vp, vp, vp, C.c_int, C.c_uint, C.c_int, vp, vp, vp],
+            "atmo_sky_radiance_to_point": [vp, vp, vp, vp, vp, C.c_int, C.c_uint, C.c_int, vp,
+                                           vp, vp],
+            "atmo_sun_and_sky_irradiance": [vp, vp, vp, vp, C.c_int, C.c_uint, C.c_int, vp, vp,
+                                            vp],
+            "atmo_solar_radiance": [vp, C.c_int, P(C.c_double)],
+            "atmo_shade_view": [vp, P(PinholeView), vp, C.c_int, vp, vp, vp],
         }
         for name, args in sigs.items():
             f = getattr(L, name)
@@ -320,6 +339,12 @@ class Model:
     def irradiance(self):
         return self._read(LUT_IRRADIANCE)
 
+    def lut_set(self) -> "LutSet":
+        """The render-time query interface of the precomputed LUTs."""
+        h = C.c_void_p()
+        _check(lib().atmo_model_lut_set(self._h, C.byref(h)))
+        return LutSet(h, self)
+
     def atmosphere_at(self, lambdas=(kLambdaR, kLambdaG, kLambdaB)) -> Atmosphere:
         a = Atmosphere()
         _check(lib().atmo_model_atmosphere_at(self._h, _dptr(lambdas), C.byref(a)))
@@ -354,6 +379,97 @@ class Model:
             _dptr(wavelengths), _dptr(spectrum), len(wavelengths), C.byref(r), C.byref(g),
             C.byref(b)))
         return r.value, g.value, b.value
+
+
+def _tensor_ptr(t, n3=None):
+    """Device pointer of a contiguous float32 CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32
+            and t.is_contiguous()):
+        raise ValueError("query arrays must be contiguous float32 CUDA tensors")
+    if n3 is not None and t.numel() != 3 * n3:
+        raise ValueError("expected %d float triples" % n3)
+    return t.data_ptr()
+
+
+class LutSet:
+    """A resident LUT set (a model after Init, or a batch instance after run)
+    and the render-time queries of the reference's shader API
+    (atmosphere/model.cc:221-281): GetSkyRadiance, GetSkyRadianceToPoint,
+    GetSunAndSkyIrradiance, GetSolarRadiance and their luminance forms, as
+    CUDA kernels over float32 CUDA tensors of shape (n, 3)."""
+
+    def __init__(self, handle, owner):
+        self._h = handle
+        self._owner = owner   # keeps the model / batch alive
+
+    def _sun(self, sun, n):
+        import torch
+        if sun.numel() == 3:
+            return sun, 0
+        _tensor_ptr(sun, n)
+        return sun, 3
+
+    def sky_radiance(self, camera, view_ray, sun_direction, shadow_length=None,
+                     luminance=False, stream=None):
+        """-> (radiance (n, 3), transmittance (n, 3)) tensors."""
+        import torch
+        n = camera.numel() // 3
+        sun, stride = self._sun(sun_direction, n)
+        out = torch.empty((n, 3), device=camera.device, dtype=torch.float32)
+        tr = torch.empty_like(out)
+        _check(lib().atmo_sky_radiance(self._h, _tensor_ptr(camera, n), _tensor_ptr(view_ray, n),
+                                       _tensor_ptr(shadow_length), _tensor_ptr(sun), stride, n,
+                                       int(bool(luminance)), out.data_ptr(), tr.data_ptr(),
+                                       _stream_ptr(stream)))
+        return out, tr
+
+    def sky_radiance_to_point(self, camera, point, sun_direction, shadow_length=None,
+                              luminance=False, stream=None):
+        import torch
+        n = camera.numel() // 3
+        sun, stride = self._sun(sun_direction, n)
+        out = torch.empty((n, 3), device=camera.device, dtype=torch.float32)
+        tr = torch.empty_like(out)
+        _check(lib().atmo_sky_radiance_to_point(
+            self._h, _tensor_ptr(camera, n), _tensor_ptr(point, n), _tensor_ptr(shadow_length),
+            _tensor_ptr(sun), stride, n, int(bool(luminance)), out.data_ptr(), tr.data_ptr(),
+            _stream_ptr(stream)))
+        return out, tr
+
+    def sun_and_sky_irradiance(self, point, normal, sun_direction, luminance=False,
+                               stream=None):
+        """-> (sun irradiance (n, 3), sky irradiance (n, 3))."""
+        import torch
+        n = point.numel() // 3
+        sun, stride = self._sun(sun_direction, n)
+        out = torch.empty((n, 3), device=point.device, dtype=torch.float32)
+        sky = torch.empty_like(out)
+        _check(lib().atmo_sun_and_sky_irradiance(
+            self._h, _tensor_ptr(point, n), _tensor_ptr(normal, n), _tensor_ptr(sun), stride, n,
+            int(bool(luminance)), out.data_ptr(), sky.data_ptr(), _stream_ptr(stream)))
+        return out, sky
+
+    def solar_radiance(self, luminance=False):
+        out = (C.c_double * 3)()
+        _check(lib().atmo_solar_radiance(self._h, int(bool(luminance)), out))
+        return tuple(out)
+
+    def shade_view(self, view: PinholeView, depth, luminance=False, stream=None):
+        """One shading request: -> (sky (H, W, 4), shaded (H, W, 4)) tensors."""
+        import torch
+        n = view.width * view.height
+        if depth.numel() != n:
+            raise ValueError("depth needs one value per pixel")
+        sky = torch.empty((view.height, view.width, 4), device=depth.device,
+                          dtype=torch.float32)
+        shaded = torch.empty_like(sky)
+        _check(lib().atmo_shade_view(self._h, C.byref(view), _tensor_ptr(depth),
+                                     int(bool(luminance)), sky.data_ptr(), shaded.data_ptr(),
+                                     _stream_ptr(stream)))
+        return sky, shaded
 
 
 def measure_fp32_peak():
@@ -402,6 +518,11 @@ class Batch:
 
     def run(self, stream=None):
         _check(lib().atmo_batch_run(self._h, _stream_ptr(stream)))
+
+    def lut_set(self, i) -> "LutSet":
+        h = C.c_void_p()
+        _check(lib().atmo_batch_lut_set(self._h, i, C.byref(h)))
+        return LutSet(h, self)
 
     def kernel_count(self):
         c = C.c_uint()

@@ -14,6 +14,7 @@
 #include "atmo_consts.h"
 #include "atmo_kernels.h"
 #include "atmo_program.h"
+#include "atmo_render.h"
 
 namespace atmo {
 const char* LastError();
@@ -109,7 +110,17 @@ struct Group {
 
 }  // namespace
 
+// A resident LUT set as the render-time queries read it.
+struct atmo_lut_set {
+  RenderLuts luts;
+  bool radiance_api = true;    // RADIANCE_API_ENABLED (3 precomputed wavelengths)
+  bool luminance_api = true;   // *_SPECTRAL_RADIANCE_TO_LUMINANCE factors known
+  double solar[3] = {0, 0, 0};
+  double sun_angular_radius = 0;
+};
+
 struct atmo_model {
+  std::unique_ptr<atmo_lut_set> lut_set;
   std::vector<double> wavelengths, solar, rayleigh, mie_sca, mie_ext, absorption, albedo;
   std::vector<atmo_density_layer> ray_layers, mie_layers, abs_layers;   // 2 each
   double sun_angular_radius = 0, bottom = 0, top = 0, g = 0, max_sun_zenith = 0, unit = 1;
@@ -217,7 +228,27 @@ struct atmo_batch {
   std::unique_ptr<Program> program;
   bool combined = true;
   bool ran = false;
+  std::vector<atmo_lut_set> lut_sets;   // per instance, filled by the first run
 };
+
+namespace {
+
+RenderLuts LutsOf(const Instance& in) {
+  RenderLuts r;
+  std::memset(&r, 0, sizeof(r));
+  r.c = in.c;
+  r.s = in.s;
+  r.T = in.T;
+  r.Tau = in.Tau;
+  r.S = in.S;
+  r.M = in.M;
+  r.I = in.I;
+  r.combined = in.combined;
+  for (int i = 0; i < 3; ++i) r.sky_k[i] = r.sun_k[i] = 1.0f;
+  return r;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -363,8 +394,23 @@ atmo_status atmo_model_init(atmo_model* m, unsigned num_scattering_orders, atmo_
     m->program_exact = m->exact;
   }
   atmo_status s = m->program->Run(st, /*use_graph=*/true);
-  if (s == ATMO_OK) m->initialized = true;
-  return s;
+  if (s != ATMO_OK) return s;
+  m->initialized = true;
+  // The shader's ATMOSPHERE constant and luminance factors (model.cc:691-744).
+  const double l[3] = {ATMO_LAMBDA_R, ATMO_LAMBDA_G, ATMO_LAMBDA_B};
+  if (!m->lut_set) m->lut_set.reset(new atmo_lut_set());
+  atmo_lut_set* set = m->lut_set.get();
+  const atmo_atmosphere a = m->AtmosphereAt(l);
+  Instance in = m->SlotFor(l, nullptr, false);
+  set->luts = LutsOf(in);
+  for (int i = 0; i < 3; ++i) {
+    set->luts.sky_k[i] = (float)(m->exact ? m->sky_k[i] : Round6(m->sky_k[i]));
+    set->luts.sun_k[i] = (float)(m->exact ? m->sun_k[i] : Round6(m->sun_k[i]));
+    set->solar[i] = a.solar_irradiance[i];
+  }
+  set->sun_angular_radius = a.sun_angular_radius;
+  set->radiance_api = m->num_precomputed_wavelengths <= 3;
+  return ATMO_OK;
 }
 
 static atmo_status ViewOf(const Storage& sto, atmo_lut_kind kind, atmo_lut_view* v) {
@@ -732,11 +778,28 @@ atmo_status atmo_batch_set_atmosphere(atmo_batch* b, unsigned i, const atmo_atmo
   return ATMO_OK;
 }
 
+static void RefreshBatchSets(atmo_batch* b) {
+  b->lut_sets.resize(b->storages.size());
+  for (size_t i = 0; i < b->storages.size(); ++i) {
+    atmo_lut_set& set = b->lut_sets[i];
+    set.luts = LutsOf(b->program->slots[i]);
+    set.luminance_api = false;
+    set.radiance_api = true;
+    const Consts& c = b->program->slots[i].c;
+    set.solar[0] = c.solar.x;
+    set.solar[1] = c.solar.y;
+    set.solar[2] = c.solar.z;
+    set.sun_angular_radius = c.alpha_s;
+  }
+}
+
 atmo_status atmo_batch_run(atmo_batch* b, atmo_stream stream) {
   if (!b) return Fail(ATMO_INVALID_ARG, "NULL batch");
   atmo_status s = b->program->Run(reinterpret_cast<cudaStream_t>(stream), /*use_graph=*/true);
-  if (s == ATMO_OK) b->ran = true;
-  return s;
+  if (s != ATMO_OK) return s;
+  b->ran = true;
+  RefreshBatchSets(b);
+  return ATMO_OK;
 }
 
 atmo_status atmo_batch_get_lut(const atmo_batch* b, unsigned i, atmo_lut_kind kind,
@@ -768,6 +831,7 @@ atmo_status atmo_batch_time_passes(atmo_batch* b, atmo_stream stream, unsigned c
   atmo_status s = b->program->TimeSteps(reinterpret_cast<cudaStream_t>(stream), &t);
   if (s != ATMO_OK) return s;
   b->ran = true;
+  RefreshBatchSets(b);
   const auto& steps = b->program->steps();
   *count = (unsigned)steps.size();
   for (size_t i = 0; i < steps.size() && i < capacity; ++i) {
@@ -784,4 +848,125 @@ atmo_status atmo_measure_fp32_peak(double* tflops) {
   return ATMO_OK;
 }
 
+
+// ---- render-time queries ----------------------------------------------------
+atmo_status atmo_model_lut_set(const atmo_model* m, const atmo_lut_set** out) {
+  if (!m || !out) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  if (!m->initialized || !m->lut_set) return Fail(ATMO_NOT_READY, "Init has not been called");
+  *out = m->lut_set.get();
+  return ATMO_OK;
+}
+
+atmo_status atmo_batch_lut_set(const atmo_batch* b, unsigned i, const atmo_lut_set** out) {
+  if (!b || !out || i >= b->storages.size()) return Fail(ATMO_INVALID_ARG, "bad argument");
+  if (!b->ran || b->lut_sets.size() != b->storages.size())
+    return Fail(ATMO_NOT_READY, "atmo_batch_run has not been called");
+  *out = &b->lut_sets[i];
+  return ATMO_OK;
+}
+
+static atmo_status CheckApi(const atmo_lut_set* set, int luminance) {
+  if (!set) return Fail(ATMO_INVALID_ARG, "NULL LUT set");
+  if (luminance && !set->luminance_api)
+    return Fail(ATMO_INVALID_ARG,
+                "no radiance-to-luminance factors for this LUT set (batch instances carry "
+                "3-wavelength atmospheres without a spectrum)");
+  if (!luminance && !set->radiance_api)
+    return Fail(ATMO_INVALID_ARG,
+                "the radiance API is not enabled with more than 3 precomputed wavelengths "
+                "(model.cc RADIANCE_API_ENABLED); use luminance = 1");
+  return ATMO_OK;
+}
+
+static atmo_status RunQuery(Query kind, const atmo_lut_set* set, const float* a, const float* b,
+                            const float* shadow, const float* sun, int sun_stride, unsigned n,
+                            int luminance, float* out0, float* out1, atmo_stream stream) {
+  atmo_status cs = CheckApi(set, luminance);
+  if (cs != ATMO_OK) return cs;
+  if (n == 0) return ATMO_OK;
+  if (!a || !b || !sun || !out0 || (sun_stride != 0 && sun_stride != 3))
+    return Fail(ATMO_INVALID_ARG, "NULL array or sun_stride not 0 or 3");
+  QueryArrays x;
+  x.a = a;
+  x.b = b;
+  x.shadow = shadow;
+  x.sun = sun;
+  x.sun_stride = sun_stride;
+  x.n = n;
+  x.luminance = luminance ? 1 : 0;
+  x.out0 = out0;
+  x.out1 = out1;
+  cudaError_t e = LaunchQuery(kind, set->luts, x, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return CudaFail(e, "query kernel launch");
+  return ATMO_OK;
+}
+
+atmo_status atmo_sky_radiance(const atmo_lut_set* set, const float* camera, const float* view_ray,
+                              const float* shadow_length, const float* sun_direction,
+                              int sun_stride, unsigned n, int luminance, float* radiance,
+                              float* transmittance, atmo_stream stream) {
+  return RunQuery(Query::kSkyRadiance, set, camera, view_ray, shadow_length, sun_direction,
+                  sun_stride, n, luminance, radiance, transmittance, stream);
+}
+
+atmo_status atmo_sky_radiance_to_point(const atmo_lut_set* set, const float* camera,
+                                       const float* point, const float* shadow_length,
+                                       const float* sun_direction, int sun_stride, unsigned n,
+                                       int luminance, float* radiance, float* transmittance,
+                                       atmo_stream stream) {
+  return RunQuery(Query::kSkyRadianceToPoint, set, camera, point, shadow_length, sun_direction,
+                  sun_stride, n, luminance, radiance, transmittance, stream);
+}
+
+atmo_status atmo_sun_and_sky_irradiance(const atmo_lut_set* set, const float* point,
+                                        const float* normal, const float* sun_direction,
+                                        int sun_stride, unsigned n, int luminance,
+                                        float* sun_irradiance, float* sky_irradiance,
+                                        atmo_stream stream) {
+  return RunQuery(Query::kSunAndSkyIrradiance, set, point, normal, nullptr, sun_direction,
+                  sun_stride, n, luminance, sun_irradiance, sky_irradiance, stream);
+}
+
+atmo_status atmo_solar_radiance(const atmo_lut_set* set, int luminance, double out[3]) {
+  atmo_status cs = CheckApi(set, luminance);
+  if (cs != ATMO_OK) return cs;
+  if (!out) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  // model.cc:226-229 and :251-255; PI as in the reference's definitions.
+  const double a = set->sun_angular_radius;
+  for (int i = 0; i < 3; ++i) {
+    out[i] = set->solar[i] / (kPiD * a * a);
+    if (luminance) out[i] *= set->luts.sun_k[i];
+  }
+  return ATMO_OK;
+}
+
+atmo_status atmo_shade_view(const atmo_lut_set* set, const atmo_pinhole_view* view,
+                            const float* depth, int luminance, float* sky_rgba,
+                            float* shaded_rgba, atmo_stream stream) {
+  atmo_status cs = CheckApi(set, luminance);
+  if (cs != ATMO_OK) return cs;
+  if (!view || !depth || !sky_rgba || !shaded_rgba)
+    return Fail(ATMO_INVALID_ARG, "NULL argument");
+  if (view->width <= 0 || view->height <= 0 || !(view->fov_y > 0.0f && view->fov_y < 3.1f))
+    return Fail(ATMO_INVALID_ARG, "bad view size or field of view");
+  PinholeView v;
+  for (int i = 0; i < 3; ++i) {
+    v.camera[i] = view->camera[i];
+    v.right[i] = view->right[i];
+    v.up[i] = view->up[i];
+    v.forward[i] = view->forward[i];
+    v.sun[i] = view->sun_direction[i];
+    v.albedo[i] = view->albedo[i];
+  }
+  v.tan_half_fov_y = std::tan(0.5f * view->fov_y);
+  v.width = view->width;
+  v.height = view->height;
+  v.depth = depth;
+  v.luminance = luminance ? 1 : 0;
+  v.sky = reinterpret_cast<float4*>(sky_rgba);
+  v.shaded = reinterpret_cast<float4*>(shaded_rgba);
+  cudaError_t e = LaunchShadeView(set->luts, v, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return CudaFail(e, "shading kernel launch");
+  return ATMO_OK;
+}
 }  // extern "C"

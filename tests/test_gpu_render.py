@@ -1,0 +1,267 @@
+"""Render-time queries (GetSkyRadiance, GetSkyRadianceToPoint,
+GetSunAndSkyIrradiance, GetSolarRadiance: atmosphere/functions.glsl:1633-1896
+behind the API of atmosphere/model.cc:221-281) on GPU-precomputed LUTs,
+against the FP64 oracle's restatement of the same functions fed the same
+LUT texels.
+
+Queries follow the serving workload: cameras at 0-100 km altitude, view and
+sun directions uniform on the sphere, points 0.1-100 km along the view ray,
+shadow lengths 0 or up to 5 km.  A query is compared only where the oracle is
+continuous: a query whose oracle value moves by more than 1e-4 when the view
+direction turns by ~2e-6 rad sits on a discontinuity of the reference itself
+(the ground / sky switch of the mu mapping at the horizon), where FP32 and
+FP64 legitimately pick different sides."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from parity import FLOOR, TOL_SCATTERING
+from test_capi_host import earth_model
+
+pytestmark = pytest.mark.gpu
+
+TOL_RENDER = TOL_SCATTERING      # per-query relative error, floor FLOOR x max
+ROBUST_STEP = 2e-6               # view-direction perturbation of the robustness mask
+ROBUST_THRESHOLD = 1e-4
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+def unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def make_queries(rng, n, rb):
+    cam = unit(rng, n) * (rb + rng.uniform(0.0, 100.0, size=(n, 1)))
+    view = unit(rng, n)
+    sun = unit(rng, n)
+    depth = rng.uniform(0.1, 100.0, size=(n, 1))
+    point = cam + view * depth
+    normal = unit(rng, n)
+    shadow = np.where(rng.random(n) < 0.5, 0.0, rng.uniform(0.0, 5.0, size=n))
+    return cam, view, sun, point, normal, shadow
+
+
+class OracleRender:
+    """The oracle's render functions over LUTs read back from the GPU."""
+
+    def __init__(self, oracle, atm, shape, T, S, M, I, combined):
+        self.O = oracle
+        self.L = oracle.lib()
+        self.atm = oracle.Atmosphere.from_buffer_copy(bytes(atm))
+        self.shp = oracle.shape(*shape)
+        self.arrays = [np.ascontiguousarray(x, np.float64) for x in (T, S, M, I)]
+        dp = oracle.dp
+        self.T, self.S, self.M, self.I = (a.ctypes.data_as(dp) for a in self.arrays)
+        self.combined = int(combined)
+
+    def _p(self, v):
+        return np.ascontiguousarray(v, np.float64).ctypes.data_as(self.O.dp)
+
+    def sky(self, cam, view, shadow, sun):
+        o, t = np.zeros(3), np.zeros(3)
+        self.L.oracle_sky_radiance(C.byref(self.atm), C.byref(self.shp), self.T, self.S, self.M,
+                                   self.combined, self._p(cam), self._p(view), float(shadow),
+                                   self._p(sun), self._p(o), self._p(t))
+        return o, t
+
+    def to_point(self, cam, point, shadow, sun):
+        o, t = np.zeros(3), np.zeros(3)
+        self.L.oracle_sky_radiance_to_point(C.byref(self.atm), C.byref(self.shp), self.T,
+                                            self.S, self.M, self.combined, self._p(cam),
+                                            self._p(point), float(shadow), self._p(sun),
+                                            self._p(o), self._p(t))
+        return o, t
+
+    def sun_sky(self, point, normal, sun):
+        a, b = np.zeros(3), np.zeros(3)
+        self.L.oracle_sun_and_sky_irradiance(C.byref(self.atm), C.byref(self.shp), self.T,
+                                             self.I, self._p(point), self._p(normal),
+                                             self._p(sun), self._p(a), self._p(b))
+        return a, b
+
+
+def oracle_outputs(ref, q, rng, perturb):
+    cam, view, sun, point, normal, shadow = q
+    n = len(cam)
+    outs = {k: np.zeros((n, 3)) for k in ("sky", "sky_t", "pt", "pt_t", "sun", "skyirr")}
+    for i in range(n):
+        v = view[i]
+        p = point[i]
+        if perturb:
+            d = rng.normal(size=3) * ROBUST_STEP
+            v = v + d
+            v = v / np.linalg.norm(v)
+            p = cam[i] + v * np.linalg.norm(point[i] - cam[i])
+        outs["sky"][i], outs["sky_t"][i] = ref.sky(cam[i], v, shadow[i], sun[i])
+        outs["pt"][i], outs["pt_t"][i] = ref.to_point(cam[i], p, shadow[i], sun[i])
+        outs["sun"][i], outs["skyirr"][i] = ref.sun_sky(point[i], normal[i], sun[i])
+    return outs
+
+
+def gpu_outputs(torch, lut_set, q):
+    cam, view, sun, point, normal, shadow = (
+        torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda() for x in q)
+    sky, sky_t = lut_set.sky_radiance(cam, view, sun, shadow)
+    pt, pt_t = lut_set.sky_radiance_to_point(cam, point, sun, shadow)
+    su, sk = lut_set.sun_and_sky_irradiance(point, normal, sun)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy().astype(np.float64) for k, v in
+            (("sky", sky), ("sky_t", sky_t), ("pt", pt), ("pt_t", pt_t), ("sun", su),
+             ("skyirr", sk))}
+
+
+def compare(ref_out, pert_out, gpu_out, what):
+    for k in ref_out:
+        o, g, p = ref_out[k], gpu_out[k], pert_out[k]
+        floor = FLOOR * max(np.abs(o).max(), 1e-30)
+        robust = np.all(np.abs(p - o) <= ROBUST_THRESHOLD * np.maximum(np.abs(o), floor),
+                        axis=1)
+        rel = np.abs(g - o) / np.maximum(np.abs(o), floor)
+        worst = rel[robust].max() if robust.any() else 0.0
+        assert robust.mean() > 0.9, (what, k, robust.mean())
+        assert np.all(np.isfinite(g)), (what, k)
+        i = int(np.argmax(np.where(robust[:, None], rel, 0.0)) // 3)
+        assert worst <= TOL_RENDER, (what, k, worst, i, g[i], o[i])
+
+
+def run_case(atmo, oracle, torch, model_or_set, atm, shape, T, S, M, I, combined, seed, n=400):
+    rng = np.random.default_rng(seed)
+    q = make_queries(rng, n, atm.bottom_radius)
+    ref = OracleRender(oracle, atm, shape, T, S, M, I, combined)
+    ref_out = oracle_outputs(ref, q, rng, False)
+    pert_out = oracle_outputs(ref, q, rng, True)
+    gpu_out = gpu_outputs(torch, model_or_set, q)
+    compare(ref_out, pert_out, gpu_out, "seed %d" % seed)
+
+
+def test_model_queries_combined_vs_oracle(atmo, oracle, torch):
+    m = earth_model(atmo)
+    m.Init(4)
+    a = m.atmosphere_at()
+    S = m.scattering()
+    run_case(atmo, oracle, torch, m.lut_set(), a, atmo.DEFAULT_SHAPE, m.transmittance(), S, S,
+             m.irradiance(), True, 11)
+
+
+def test_model_queries_separate_textures_vs_oracle(atmo, oracle, torch):
+    shape = oracle.MEDIUM_SHAPE
+    m = earth_model(atmo, combined=False, shape=shape)
+    m.Init(4)
+    a = m.atmosphere_at()
+    run_case(atmo, oracle, torch, m.lut_set(), a, shape, m.transmittance(), m.scattering(),
+             m.single_mie_scattering(), m.irradiance(), False, 12)
+
+
+def test_batch_instance_queries_vs_oracle(atmo, oracle, torch):
+    from test_gpu_parity import random_atmosphere
+    rng = np.random.default_rng(21)
+    atms = [random_atmosphere(oracle, rng) for _ in range(2)]
+    shape = oracle.MEDIUM_SHAPE
+    b = atmo.Batch(atms, [shape] * 2, [3, 4])
+    b.run()
+    atmo.synchronize_stream()
+    i = 1
+    S = b.read(i, atmo.LUT_SCATTERING)
+    run_case(atmo, oracle, torch, b.lut_set(i), atms[i], shape,
+             b.read(i, atmo.LUT_TRANSMITTANCE), S, S, b.read(i, atmo.LUT_IRRADIANCE), True, 13,
+             n=200)
+    with pytest.raises(atmo.AtmoError):
+        b.lut_set(i).solar_radiance(luminance=True)
+
+
+def test_luminance_api_and_solar_radiance(atmo, torch):
+    m = earth_model(atmo)
+    m.Init(4)
+    s = m.lut_set()
+    sky_k, sun_k = m.luminance_factors()
+    a = m.atmosphere_at()
+    r = s.solar_radiance()
+    for i in range(3):
+        assert r[i] == pytest.approx(a.solar_irradiance[i] / (np.pi * a.sun_angular_radius ** 2),
+                                     rel=1e-12)
+    rl = s.solar_radiance(luminance=True)
+    k6 = [float("%.6f" % k) for k in sun_k]
+    for i in range(3):
+        assert rl[i] == pytest.approx(r[i] * k6[i], rel=1e-6)
+    rng = np.random.default_rng(3)
+    cam, view, sun, point, normal, shadow = (
+        torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+        for x in make_queries(rng, 256, 6360.0))
+    rad, _ = s.sky_radiance(cam, view, sun)
+    lum, _ = s.sky_radiance(cam, view, sun, luminance=True)
+    ks = torch.tensor([float("%.6f" % k) for k in sky_k], device="cuda")
+    torch.testing.assert_close(lum, rad * ks, rtol=1e-6, atol=0.0)
+    a1, b1 = s.sun_and_sky_irradiance(point, normal, sun)
+    a2, b2 = s.sun_and_sky_irradiance(point, normal, sun, luminance=True)
+    ksun = torch.tensor(k6, device="cuda")
+    torch.testing.assert_close(a2, a1 * ksun, rtol=1e-6, atol=0.0)
+    torch.testing.assert_close(b2, b1 * ks, rtol=1e-6, atol=0.0)
+    # One sun direction for every query equals the per-query form.
+    one = sun[0].contiguous()
+    r1, _ = s.sky_radiance(cam, view, one)
+    r2, _ = s.sky_radiance(cam, view, one.expand_as(sun).contiguous())
+    torch.testing.assert_close(r1, r2, rtol=0.0, atol=0.0)
+
+
+def test_fifteen_wavelength_model_has_luminance_api_only(atmo, torch):
+    m = earth_model(atmo, n_lambda=15)
+    m.Init(2)
+    s = m.lut_set()
+    v = torch.tensor([[0.0, 0.0, 6361.0]], device="cuda")
+    d = torch.tensor([[0.0, 0.6, 0.8]], device="cuda")
+    sun = torch.tensor([0.0, 0.0, 1.0], device="cuda")
+    lum, _ = s.sky_radiance(v, d, sun, luminance=True)
+    assert torch.isfinite(lum).all() and (lum > 0).all()
+    with pytest.raises(atmo.AtmoError):
+        s.sky_radiance(v, d, sun, luminance=False)
+
+
+def test_shade_view_equals_queries(atmo, torch):
+    m = earth_model(atmo)
+    m.Init(4)
+    s = m.lut_set()
+    W, H = 64, 48
+    cam = np.array([0.0, 0.0, 6360.0 + 1.5])
+    fwd = np.array([0.0, 0.9, 0.1]); fwd /= np.linalg.norm(fwd)
+    right = np.cross(fwd, [0.0, 0.0, 1.0]); right /= np.linalg.norm(right)
+    up = np.cross(right, fwd)
+    sun = np.array([0.3, 0.5, 0.4]); sun /= np.linalg.norm(sun)
+    view = atmo.PinholeView()
+    for name, v in (("camera", cam), ("right", right), ("up", up), ("forward", fwd),
+                    ("sun_direction", sun), ("albedo", [0.1, 0.2, 0.3])):
+        setattr(view, name, (C.c_float * 3)(*v))
+    view.fov_y = np.radians(50.0)
+    view.width, view.height = W, H
+    rng = np.random.default_rng(5)
+    depth = rng.uniform(0.1, 100.0, size=(H, W)).astype(np.float32)
+    dt = torch.from_numpy(depth).cuda()
+    sky, shaded = s.shade_view(view, dt)
+    # The same pixels through the query kernels, with the rays built here.
+    f32 = lambda x: np.asarray(x, np.float32)  # noqa: E731
+    t = np.float32(np.tan(np.float32(0.5 * np.float32(view.fov_y))))
+    ii, jj = np.meshgrid(np.arange(W), np.arange(H))
+    sx = ((2 * ii + 1) / np.float32(W) - 1) * t * (np.float32(W) / np.float32(H))
+    sy = (1 - (2 * jj + 1) / np.float32(H)) * t
+    rays = f32(fwd)[None, None] + sx[..., None] * f32(right) + sy[..., None] * f32(up)
+    rays /= np.linalg.norm(rays, axis=-1, keepdims=True)
+    rays = torch.from_numpy(f32(rays.reshape(-1, 3))).cuda()
+    camt = torch.from_numpy(f32(np.tile(cam, (W * H, 1)))).cuda()
+    sunt = torch.from_numpy(f32(sun)).cuda()
+    r_sky, t_sky = s.sky_radiance(camt, rays, sunt)
+    pts = camt + rays * dt.reshape(-1, 1)
+    r_pt, t_pt = s.sky_radiance_to_point(camt, pts, sunt)
+    su, sk = s.sun_and_sky_irradiance(pts, -rays, sunt)
+    alb = torch.tensor([0.1, 0.2, 0.3], device="cuda") / np.pi
+    expect = r_pt + t_pt * alb * (su + sk)
+    torch.testing.assert_close(sky.reshape(-1, 4)[:, :3], r_sky, rtol=2e-4, atol=1e-7)
+    torch.testing.assert_close(sky.reshape(-1, 4)[:, 3], t_sky[:, 1], rtol=2e-4, atol=1e-7)
+    torch.testing.assert_close(shaded.reshape(-1, 4)[:, :3], expect, rtol=2e-4, atol=1e-7)
