@@ -137,7 +137,10 @@ void GpuChecks() {
         finite = finite && std::isfinite(x);
         nonneg = nonneg && x >= 0.0f;
       }
-      Expect(finite && nonneg, "LUT texels are finite and non-negative");
+      Expect(finite, "LUT texels are finite");
+      // Radiance LUTs are non-negative; luminance LUTs (more than 3
+      // wavelengths) hold linear sRGB, whose components can be negative.
+      Expect(nonneg || n_lambda > 3, "radiance LUT texels are non-negative");
     }
     const atmo_lut_view s = facade->lut(ATMO_LUT_SCATTERING);
     Expect(s.width == 256 && s.height == 128 && s.depth == 32,
