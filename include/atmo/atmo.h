@@ -325,6 +325,22 @@ typedef struct {
 atmo_status atmo_shade_view(const atmo_lut_set* set, const atmo_pinhole_view* view,
                             const float* depth, int luminance, float* sky_rgba,
                             float* shaded_rgba, atmo_stream stream);
+/* ---- LUT files -------------------------------------------------------------- */
+/* Writes the LUTs the way the reference's precompute tool does
+   (atmosphere/demo/webgl/precompute.cc:63-106, read by demo.js:364-377): raw
+   little-endian float32 RGBA texels, x fastest, in transmittance.dat,
+   scattering.dat, irradiance.dat and, for a model, the shader source in
+   atmosphere_shader.txt; also single_mie_scattering.dat when the textures are
+   not combined and optical_depth.dat (this library's -ln T LUT, used for
+   ratios of transmittances below FP32's normal range).  `directory` must
+   exist.  Synchronous. */
+atmo_status atmo_model_save_luts(const atmo_model* model, const char* directory);
+atmo_status atmo_batch_save_luts(const atmo_batch* batch, unsigned i, const char* directory);
+/* Loads LUT files into a model as if atmo_model_init had computed them (a
+   cache or checkpoint: render-time queries work without a rebuild).  Sizes
+   must match the model's LUT shape; without optical_depth.dat (files of the
+   reference's tool) -ln T stands in for it.  Synchronous. */
+atmo_status atmo_model_load_luts(atmo_model* model, const char* directory);
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Measures this GPU's FP32 FMA throughput (TFLOP/s, 2 FLOP per FMA) with a
    short dependent-chain kernel over every SM: the denominator of the

@@ -198,6 +198,9 @@ def lib():
                                             vp],
             "atmo_solar_radiance": [vp, C.c_int, P(C.c_double)],
             "atmo_shade_view": [vp, P(PinholeView), vp, C.c_int, vp, vp, vp],
+            "atmo_model_save_luts": [vp, C.c_char_p],
+            "atmo_model_load_luts": [vp, C.c_char_p],
+            "atmo_batch_save_luts": [vp, C.c_uint, C.c_char_p],
         }
         for name, args in sigs.items():
             f = getattr(L, name)
@@ -338,6 +341,15 @@ class Model:
 
     def irradiance(self):
         return self._read(LUT_IRRADIANCE)
+
+    def save_luts(self, directory):
+        """transmittance.dat, scattering.dat, irradiance.dat (raw float32 RGBA,
+        atmosphere/demo/webgl/precompute.cc:63-106) and atmosphere_shader.txt."""
+        _check(lib().atmo_model_save_luts(self._h, os.fsencode(directory)))
+
+    def load_luts(self, directory):
+        """Makes the model ready from LUT files instead of Init."""
+        _check(lib().atmo_model_load_luts(self._h, os.fsencode(directory)))
 
     def lut_set(self) -> "LutSet":
         """The render-time query interface of the precomputed LUTs."""
@@ -518,6 +530,9 @@ class Batch:
 
     def run(self, stream=None):
         _check(lib().atmo_batch_run(self._h, _stream_ptr(stream)))
+
+    def save_luts(self, i, directory):
+        _check(lib().atmo_batch_save_luts(self._h, i, os.fsencode(directory)))
 
     def lut_set(self, i) -> "LutSet":
         h = C.c_void_p()

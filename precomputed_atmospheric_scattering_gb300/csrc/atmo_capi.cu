@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <string>
 #include <vector>
@@ -363,6 +364,24 @@ atmo_status atmo_model_set_exact_parameters(atmo_model* m, int exact) {
   return ATMO_OK;
 }
 
+// The shader's ATMOSPHERE constant and luminance factors (model.cc:691-744)
+// over the model's LUTs.
+static void BuildModelLutSet(atmo_model* m) {
+  const double l[3] = {ATMO_LAMBDA_R, ATMO_LAMBDA_G, ATMO_LAMBDA_B};
+  if (!m->lut_set) m->lut_set.reset(new atmo_lut_set());
+  atmo_lut_set* set = m->lut_set.get();
+  const atmo_atmosphere a = m->AtmosphereAt(l);
+  Instance in = m->SlotFor(l, nullptr, false);
+  set->luts = LutsOf(in);
+  for (int i = 0; i < 3; ++i) {
+    set->luts.sky_k[i] = (float)(m->exact ? m->sky_k[i] : Round6(m->sky_k[i]));
+    set->luts.sun_k[i] = (float)(m->exact ? m->sun_k[i] : Round6(m->sun_k[i]));
+    set->solar[i] = a.solar_irradiance[i];
+  }
+  set->sun_angular_radius = a.sun_angular_radius;
+  set->radiance_api = m->num_precomputed_wavelengths <= 3;
+}
+
 atmo_status atmo_model_init(atmo_model* m, unsigned num_scattering_orders, atmo_stream stream) {
   if (!m) return Fail(ATMO_INVALID_ARG, "NULL model");
   if (num_scattering_orders < 1 || num_scattering_orders > 64)
@@ -396,20 +415,7 @@ atmo_status atmo_model_init(atmo_model* m, unsigned num_scattering_orders, atmo_
   atmo_status s = m->program->Run(st, /*use_graph=*/true);
   if (s != ATMO_OK) return s;
   m->initialized = true;
-  // The shader's ATMOSPHERE constant and luminance factors (model.cc:691-744).
-  const double l[3] = {ATMO_LAMBDA_R, ATMO_LAMBDA_G, ATMO_LAMBDA_B};
-  if (!m->lut_set) m->lut_set.reset(new atmo_lut_set());
-  atmo_lut_set* set = m->lut_set.get();
-  const atmo_atmosphere a = m->AtmosphereAt(l);
-  Instance in = m->SlotFor(l, nullptr, false);
-  set->luts = LutsOf(in);
-  for (int i = 0; i < 3; ++i) {
-    set->luts.sky_k[i] = (float)(m->exact ? m->sky_k[i] : Round6(m->sky_k[i]));
-    set->luts.sun_k[i] = (float)(m->exact ? m->sun_k[i] : Round6(m->sun_k[i]));
-    set->solar[i] = a.solar_irradiance[i];
-  }
-  set->sun_angular_radius = a.sun_angular_radius;
-  set->radiance_api = m->num_precomputed_wavelengths <= 3;
+  BuildModelLutSet(m);
   return ATMO_OK;
 }
 
@@ -968,5 +974,151 @@ atmo_status atmo_shade_view(const atmo_lut_set* set, const atmo_pinhole_view* vi
   cudaError_t e = LaunchShadeView(set->luts, v, reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return CudaFail(e, "shading kernel launch");
   return ATMO_OK;
+}
+
+// ---- LUT files (atmosphere/demo/webgl/precompute.cc:63-106) ------------------
+static std::string JoinPath(const char* dir, const char* name) {
+  std::string d(dir);
+  if (!d.empty() && d.back() != '/') d += '/';
+  return d + name;
+}
+
+static atmo_status WriteFile(const std::string& path, const void* data, size_t bytes) {
+  std::ofstream out(path, std::ofstream::out | std::ofstream::binary);
+  if (!out) return Fail(ATMO_INVALID_ARG, "cannot open " + path + " for writing");
+  out.write(static_cast<const char*>(data), (std::streamsize)bytes);
+  if (!out) return Fail(ATMO_INVALID_ARG, "cannot write " + path);
+  return ATMO_OK;
+}
+
+// Reads exactly `bytes` bytes; *present = false when the file does not exist.
+static atmo_status ReadFile(const std::string& path, size_t bytes, std::vector<float>* out,
+                            bool* present) {
+  std::ifstream in(path, std::ifstream::in | std::ifstream::binary);
+  if (present) *present = (bool)in;
+  if (!in) {
+    if (present) return ATMO_OK;
+    return Fail(ATMO_INVALID_ARG, "cannot open " + path);
+  }
+  in.seekg(0, std::ios::end);
+  const std::streamoff size = in.tellg();
+  if (size < 0 || (size_t)size != bytes)
+    return Fail(ATMO_INVALID_ARG, path + " has " + std::to_string((long long)size) +
+                                      " bytes, the LUT shape needs " + std::to_string(bytes));
+  in.seekg(0, std::ios::beg);
+  out->resize(bytes / sizeof(float));
+  in.read(reinterpret_cast<char*>(out->data()), (std::streamsize)bytes);
+  if (!in) return Fail(ATMO_INVALID_ARG, "cannot read " + path);
+  return ATMO_OK;
+}
+
+static atmo_status SaveStorage(const Storage& sto, const char* dir, const std::string* shader) {
+  if (!dir) return Fail(ATMO_INVALID_ARG, "NULL directory");
+  struct Item {
+    atmo_lut_kind kind;
+    const char* name;
+  };
+  std::vector<Item> items = {{ATMO_LUT_TRANSMITTANCE, "transmittance.dat"},
+                             {ATMO_LUT_SCATTERING, "scattering.dat"},
+                             {ATMO_LUT_IRRADIANCE, "irradiance.dat"}};
+  if (!sto.combined) items.push_back({ATMO_LUT_SINGLE_MIE, "single_mie_scattering.dat"});
+  std::vector<float> host;
+  for (const Item& it : items) {
+    atmo_lut_view v;
+    atmo_status s = ViewOf(sto, it.kind, &v);
+    if (s != ATMO_OK) return s;
+    host.resize((size_t)v.width * v.height * v.depth * 4);
+    if ((s = ReadView(v, host.data(), host.size() * sizeof(float))) != ATMO_OK) return s;
+    if ((s = WriteFile(JoinPath(dir, it.name), host.data(), host.size() * sizeof(float))) !=
+        ATMO_OK)
+      return s;
+  }
+  // This library's optical-depth LUT, so that a reload keeps the ratios of
+  // transmittances below FP32's normal range.
+  host.resize((size_t)sto.s.t_texels() * 4);
+  ATMO_CUDA_TRY(
+      cudaMemcpy(host.data(), sto.Tau, host.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  atmo_status s = WriteFile(JoinPath(dir, "optical_depth.dat"), host.data(),
+                            host.size() * sizeof(float));
+  if (s != ATMO_OK) return s;
+  if (shader) s = WriteFile(JoinPath(dir, "atmosphere_shader.txt"), shader->data(), shader->size());
+  return s;
+}
+
+static atmo_status LoadStorage(Storage& sto, const char* dir) {
+  if (!dir) return Fail(ATMO_INVALID_ARG, "NULL directory");
+  const Shape& sh = sto.s;
+  const size_t t_bytes = (size_t)sh.t_texels() * 16, s_bytes = (size_t)sh.s_texels() * 16,
+               i_bytes = (size_t)sh.i_texels() * 16;
+  std::vector<float> T, S, M, I, Tau;
+  atmo_status s;
+  // Every file is read and checked before any device buffer changes.
+  if ((s = ReadFile(JoinPath(dir, "transmittance.dat"), t_bytes, &T, nullptr)) != ATMO_OK)
+    return s;
+  if ((s = ReadFile(JoinPath(dir, "scattering.dat"), s_bytes, &S, nullptr)) != ATMO_OK) return s;
+  if ((s = ReadFile(JoinPath(dir, "irradiance.dat"), i_bytes, &I, nullptr)) != ATMO_OK) return s;
+  if (!sto.combined &&
+      (s = ReadFile(JoinPath(dir, "single_mie_scattering.dat"), s_bytes, &M, nullptr)) != ATMO_OK)
+    return s;
+  bool have_tau = false;
+  if ((s = ReadFile(JoinPath(dir, "optical_depth.dat"), t_bytes, &Tau, &have_tau)) != ATMO_OK)
+    return s;
+  if (!have_tau) {
+    // Files of the reference's tool: the optical depth from T itself.
+    Tau.resize(T.size());
+    for (size_t i = 0; i < T.size(); ++i)
+      Tau[i] = (i % 4 == 3) ? 0.0f : -std::log(std::fmax(T[i], 1.17549435e-38f));
+  }
+  ATMO_CUDA_TRY(cudaMemcpy(sto.T, T.data(), t_bytes, cudaMemcpyHostToDevice));
+  ATMO_CUDA_TRY(cudaMemcpy(sto.Tau, Tau.data(), t_bytes, cudaMemcpyHostToDevice));
+  ATMO_CUDA_TRY(cudaMemcpy(sto.S, S.data(), s_bytes, cudaMemcpyHostToDevice));
+  ATMO_CUDA_TRY(cudaMemcpy(sto.I, I.data(), i_bytes, cudaMemcpyHostToDevice));
+  if (!sto.combined) ATMO_CUDA_TRY(cudaMemcpy(sto.M, M.data(), s_bytes, cudaMemcpyHostToDevice));
+  if (sto.half) {
+    cudaError_t e = LaunchToHalf(sto.S, sto.S_half, sh.s_texels(), nullptr);
+    if (e == cudaSuccess && !sto.combined) e = LaunchToHalf(sto.M, sto.M_half, sh.s_texels(), nullptr);
+    if (e != cudaSuccess) return CudaFail(e, "FP16 conversion");
+  }
+  ATMO_CUDA_TRY(cudaDeviceSynchronize());
+  return ATMO_OK;
+}
+
+atmo_status atmo_model_save_luts(const atmo_model* m, const char* directory) {
+  if (!m) return Fail(ATMO_INVALID_ARG, "NULL model");
+  if (!m->initialized) return Fail(ATMO_NOT_READY, "Init has not been called");
+  size_t need = 0;
+  atmo_status s = atmo_model_shader_source(m, nullptr, 0, &need);
+  if (s != ATMO_OK) return s;
+  std::string shader(need, '\0');
+  if ((s = atmo_model_shader_source(m, &shader[0], need, &need)) != ATMO_OK) return s;
+  shader.resize(need > 0 ? need - 1 : 0);
+  return SaveStorage(m->storage, directory, &shader);
+}
+
+atmo_status atmo_model_load_luts(atmo_model* m, const char* directory) {
+  if (!m) return Fail(ATMO_INVALID_ARG, "NULL model");
+  // Size checks first: they need no device.
+  const Shape sh = ToShape(m->shape);
+  const size_t t_bytes = (size_t)sh.t_texels() * 16, s_bytes = (size_t)sh.s_texels() * 16,
+               i_bytes = (size_t)sh.i_texels() * 16;
+  std::vector<float> probe;
+  atmo_status s;
+  if ((s = ReadFile(JoinPath(directory ? directory : "", "transmittance.dat"), t_bytes, &probe,
+                    nullptr)) != ATMO_OK ||
+      (s = ReadFile(JoinPath(directory ? directory : "", "irradiance.dat"), i_bytes, &probe,
+                    nullptr)) != ATMO_OK)
+    return s;
+  (void)s_bytes;
+  if ((s = EnsureStorage(m)) != ATMO_OK) return s;
+  if ((s = LoadStorage(m->storage, directory)) != ATMO_OK) return s;
+  m->initialized = true;
+  BuildModelLutSet(m);
+  return ATMO_OK;
+}
+
+atmo_status atmo_batch_save_luts(const atmo_batch* b, unsigned i, const char* directory) {
+  if (!b || i >= b->storages.size()) return Fail(ATMO_INVALID_ARG, "bad argument");
+  if (!b->ran) return Fail(ATMO_NOT_READY, "atmo_batch_run has not been called");
+  return SaveStorage(b->storages[i], directory, nullptr);
 }
 }  // extern "C"
