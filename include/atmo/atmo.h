@@ -153,6 +153,7 @@ typedef enum { ATMO_PATH_FAST = 0, ATMO_PATH_PLAIN = 1 } atmo_path;
 typedef struct atmo_model atmo_model;
 typedef struct atmo_batch atmo_batch;
 typedef struct atmo_lut_set atmo_lut_set;
+typedef struct atmo_server atmo_server;
 
 /* ---- library --------------------------------------------------------------- */
 int atmo_abi_version(void);
@@ -304,6 +305,10 @@ atmo_status atmo_sun_and_sky_irradiance(const atmo_lut_set* set, const float* po
                                         int sun_stride, unsigned n, int luminance,
                                         float* sun_irradiance, float* sky_irradiance,
                                         atmo_stream stream);
+/* Copies a LUT of the set to host memory (float32 RGBA; bytes = texels x 16;
+   the scattering LUT is read in float32).  Synchronous. */
+atmo_status atmo_lut_set_read(const atmo_lut_set* set, atmo_lut_kind kind, float* host_dst,
+                              size_t bytes);
 /* GetSolarRadiance / GetSolarLuminance (host). */
 atmo_status atmo_solar_radiance(const atmo_lut_set* set, int luminance, double out[3]);
 /* A pinhole view: pixel (i, j) of width x height (row j from the top) looks
@@ -341,6 +346,60 @@ atmo_status atmo_batch_save_luts(const atmo_batch* batch, unsigned i, const char
    must match the model's LUT shape; without optical_depth.dat (files of the
    reference's tool) -ln T stands in for it.  Synchronous. */
 atmo_status atmo_model_load_luts(atmo_model* model, const char* directory);
+/* ---- serving ------------------------------------------------------------------ */
+/* A request loop over resident LUT sets (no counterpart in the reference,
+   whose Model is one synchronous precomputation): rebuild requests are
+   admitted while their final LUTs and temporaries fit hbm_budget_bytes,
+   evicting idle ready sets least recently used first, and are batched at
+   pass granularity with the rebuilds already running (uneven LUT shapes and
+   order counts in one launch); shading requests (atmo_shade_view on a ready
+   set) run on their own streams beside the rebuilds.  A result is the same
+   alone and in any mix.  Sets are 3-wavelength radiance sets (FP32).  All
+   calls are thread-safe; waits are bounded by their timeout. */
+typedef struct {
+  size_t hbm_budget_bytes;           /* 0: 120 GiB */
+  unsigned max_rebuilds_in_flight;   /* admitted, not yet built (0: 64; <= 4096) */
+  unsigned shade_streams;            /* 0: 4 */
+  int combined;                      /* combine_scattering_textures of every set */
+} atmo_server_config;
+typedef struct {
+  int state;             /* 0 queued, 1 running, 2 done, 3 failed */
+  atmo_status status;    /* of a failed request (ATMO_BUDGET, ATMO_NOT_READY ...) */
+  double queue_ms;       /* submission to admission / launch (-1 while queued) */
+  double latency_ms;     /* submission to completion on the GPU (-1 before) */
+  uint64_t set_id;       /* the LUT set (a rebuild's own ticket) */
+} atmo_ticket_info;
+typedef struct {
+  size_t used_bytes, budget_bytes;
+  unsigned resident_sets, building, pending;
+  unsigned long long evictions, rounds, kernels, shades_launched;
+} atmo_server_stats;
+atmo_status atmo_server_create(const atmo_server_config* config, atmo_server** out);
+/* Waits for the work in flight, then frees every set. */
+atmo_status atmo_server_destroy(atmo_server* server);
+/* A rebuild of `atmosphere` (shape may be NULL); the ticket doubles as the
+   LUT set's id. */
+atmo_status atmo_server_submit_rebuild(atmo_server* server, const atmo_atmosphere* atmosphere,
+                                       const atmo_lut_shape* shape, unsigned num_scattering_orders,
+                                       uint64_t* ticket);
+/* A shading request on set `set_id` (it runs once the set is built); depth,
+   sky_rgba and shaded_rgba are device buffers (atmo_shade_view) that the
+   caller keeps alive until the ticket completes. */
+atmo_status atmo_server_submit_shade(atmo_server* server, uint64_t set_id,
+                                     const atmo_pinhole_view* view, const float* depth,
+                                     float* sky_rgba, float* shaded_rgba, uint64_t* ticket);
+atmo_status atmo_server_poll(atmo_server* server, uint64_t ticket, atmo_ticket_info* info);
+/* ATMO_OK when done (for a rebuild: its set is ready), the request's status
+   when it failed, ATMO_TIMEOUT after timeout_ms. */
+atmo_status atmo_server_wait(atmo_server* server, uint64_t ticket, unsigned timeout_ms,
+                             atmo_ticket_info* info);
+/* Forgets a completed shading ticket (rebuild tickets go with their set). */
+atmo_status atmo_server_release_ticket(atmo_server* server, uint64_t ticket);
+/* The render-time query interface of a ready set (marks it used). */
+atmo_status atmo_server_lut_set(atmo_server* server, uint64_t set_id, const atmo_lut_set** out);
+/* Frees a ready, idle set now. */
+atmo_status atmo_server_evict(atmo_server* server, uint64_t set_id);
+atmo_status atmo_server_get_stats(atmo_server* server, atmo_server_stats* out);
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Measures this GPU's FP32 FMA throughput (TFLOP/s, 2 FLOP per FMA) with a
    short dependent-chain kernel over every SM: the denominator of the

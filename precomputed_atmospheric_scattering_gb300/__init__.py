@@ -128,6 +128,23 @@ class PinholeView(C.Structure):
                 ("sun_direction", _F3), ("albedo", _F3)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_rebuilds_in_flight", C.c_uint),
+                ("shade_streams", C.c_uint), ("combined", C.c_int)]
+
+
+class TicketInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("status", C.c_int), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("set_id", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("used_bytes", C.c_size_t), ("budget_bytes", C.c_size_t),
+                ("resident_sets", C.c_uint), ("building", C.c_uint), ("pending", C.c_uint),
+                ("evictions", C.c_ulonglong), ("rounds", C.c_ulonglong),
+                ("kernels", C.c_ulonglong), ("shades_launched", C.c_ulonglong)]
+
+
 class LutView(C.Structure):
     _fields_ = [("device_ptr", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
                 ("depth", C.c_int), ("dtype", C.c_int), ("bytes", C.c_size_t)]
@@ -198,6 +215,19 @@ def lib():
                                             vp],
             "atmo_solar_radiance": [vp, C.c_int, P(C.c_double)],
             "atmo_shade_view": [vp, P(PinholeView), vp, C.c_int, vp, vp, vp],
+            "atmo_lut_set_read": [vp, C.c_int, P(C.c_float), C.c_size_t],
+            "atmo_server_create": [P(ServerConfig), P(vp)],
+            "atmo_server_destroy": [vp],
+            "atmo_server_submit_rebuild": [vp, P(Atmosphere), P(LutShape), C.c_uint,
+                                           P(C.c_uint64)],
+            "atmo_server_submit_shade": [vp, C.c_uint64, P(PinholeView), vp, vp, vp,
+                                         P(C.c_uint64)],
+            "atmo_server_poll": [vp, C.c_uint64, P(TicketInfo)],
+            "atmo_server_wait": [vp, C.c_uint64, C.c_uint, P(TicketInfo)],
+            "atmo_server_release_ticket": [vp, C.c_uint64],
+            "atmo_server_lut_set": [vp, C.c_uint64, P(vp)],
+            "atmo_server_evict": [vp, C.c_uint64],
+            "atmo_server_get_stats": [vp, P(ServerStats)],
             "atmo_model_save_luts": [vp, C.c_char_p],
             "atmo_model_load_luts": [vp, C.c_char_p],
             "atmo_batch_save_luts": [vp, C.c_uint, C.c_char_p],
@@ -355,7 +385,7 @@ class Model:
         """The render-time query interface of the precomputed LUTs."""
         h = C.c_void_p()
         _check(lib().atmo_model_lut_set(self._h, C.byref(h)))
-        return LutSet(h, self)
+        return LutSet(h, self, self._shape.as_tuple())
 
     def atmosphere_at(self, lambdas=(kLambdaR, kLambdaG, kLambdaB)) -> Atmosphere:
         a = Atmosphere()
@@ -413,9 +443,10 @@ class LutSet:
     GetSunAndSkyIrradiance, GetSolarRadiance and their luminance forms, as
     CUDA kernels over float32 CUDA tensors of shape (n, 3)."""
 
-    def __init__(self, handle, owner):
+    def __init__(self, handle, owner, shape=None):
         self._h = handle
-        self._owner = owner   # keeps the model / batch alive
+        self._owner = owner   # keeps the model / batch / server alive
+        self._owner_shape = tuple(shape) if shape is not None else None
 
     def _sun(self, sun, n):
         import torch
@@ -464,6 +495,22 @@ class LutSet:
             int(bool(luminance)), out.data_ptr(), sky.data_ptr(), _stream_ptr(stream)))
         return out, sky
 
+    def read(self, kind):
+        """A LUT of the set as a host array (transmittance / irradiance (H, W, 4),
+        scattering (R, MU, NU*MU_S, 4))."""
+        sh = self._shape()
+        if kind in (LUT_TRANSMITTANCE, LUT_IRRADIANCE):
+            w, h = ((sh[0], sh[1]) if kind == LUT_TRANSMITTANCE else (sh[6], sh[7]))
+            out = np.empty((h, w, 4), np.float32)
+        else:
+            out = np.empty((sh[2], sh[3], sh[5] * sh[4], 4), np.float32)
+        _check(lib().atmo_lut_set_read(self._h, kind, out.ctypes.data_as(C.POINTER(C.c_float)),
+                                       out.nbytes))
+        return out
+
+    def _shape(self):
+        return self._owner_shape
+
     def solar_radiance(self, luminance=False):
         out = (C.c_double * 3)()
         _check(lib().atmo_solar_radiance(self._h, int(bool(luminance)), out))
@@ -482,6 +529,74 @@ class LutSet:
                                      int(bool(luminance)), sky.data_ptr(), shaded.data_ptr(),
                                      _stream_ptr(stream)))
         return sky, shaded
+
+
+class Server:
+    """The serving engine (atmo_server_*): resident LUT sets under an HBM
+    budget with LRU eviction, rebuilds batched at pass granularity, shading
+    requests on their own streams."""
+
+    QUEUED, RUNNING, DONE, FAILED = range(4)
+
+    def __init__(self, hbm_budget_bytes=0, max_rebuilds_in_flight=0, shade_streams=0,
+                 combined=True):
+        cfg = ServerConfig(hbm_budget_bytes, max_rebuilds_in_flight, shade_streams,
+                           int(bool(combined)))
+        h = C.c_void_p()
+        _check(lib().atmo_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._shapes = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.atmo_server_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def submit_rebuild(self, atmosphere, shape=None, orders=4):
+        a = Atmosphere.from_buffer_of(atmosphere)
+        s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+        t = C.c_uint64()
+        _check(lib().atmo_server_submit_rebuild(self._h, C.byref(a), C.byref(s), orders,
+                                                C.byref(t)))
+        self._shapes[t.value] = s.as_tuple()
+        return t.value
+
+    def submit_shade(self, set_id, view, depth, sky, shaded):
+        """view: PinholeView; depth (H*W) and sky / shaded (H, W, 4) float32
+        CUDA tensors kept alive by the caller until the ticket completes."""
+        t = C.c_uint64()
+        _check(lib().atmo_server_submit_shade(self._h, set_id, C.byref(view),
+                                              _tensor_ptr(depth), _tensor_ptr(sky),
+                                              _tensor_ptr(shaded), C.byref(t)))
+        return t.value
+
+    def poll(self, ticket) -> TicketInfo:
+        info = TicketInfo()
+        _check(lib().atmo_server_poll(self._h, ticket, C.byref(info)))
+        return info
+
+    def wait(self, ticket, timeout_ms=60000) -> TicketInfo:
+        info = TicketInfo()
+        _check(lib().atmo_server_wait(self._h, ticket, timeout_ms, C.byref(info)))
+        return info
+
+    def release_ticket(self, ticket):
+        _check(lib().atmo_server_release_ticket(self._h, ticket))
+
+    def lut_set(self, set_id) -> LutSet:
+        h = C.c_void_p()
+        _check(lib().atmo_server_lut_set(self._h, set_id, C.byref(h)))
+        return LutSet(h, self, self._shapes.get(set_id))
+
+    def evict(self, set_id):
+        _check(lib().atmo_server_evict(self._h, set_id))
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(lib().atmo_server_get_stats(self._h, C.byref(s)))
+        return s
 
 
 def measure_fp32_peak():
@@ -537,7 +652,7 @@ class Batch:
     def lut_set(self, i) -> "LutSet":
         h = C.c_void_p()
         _check(lib().atmo_batch_lut_set(self._h, i, C.byref(h)))
-        return LutSet(h, self)
+        return LutSet(h, self, self.shapes[i].as_tuple())
 
     def kernel_count(self):
         c = C.c_uint()

@@ -111,15 +111,6 @@ struct Group {
 
 }  // namespace
 
-// A resident LUT set as the render-time queries read it.
-struct atmo_lut_set {
-  RenderLuts luts;
-  bool radiance_api = true;    // RADIANCE_API_ENABLED (3 precomputed wavelengths)
-  bool luminance_api = true;   // *_SPECTRAL_RADIANCE_TO_LUMINANCE factors known
-  double solar[3] = {0, 0, 0};
-  double sun_angular_radius = 0;
-};
-
 struct atmo_model {
   std::unique_ptr<atmo_lut_set> lut_set;
   std::vector<double> wavelengths, solar, rayleigh, mie_sca, mie_ext, absorption, albedo;
@@ -232,24 +223,7 @@ struct atmo_batch {
   std::vector<atmo_lut_set> lut_sets;   // per instance, filled by the first run
 };
 
-namespace {
 
-RenderLuts LutsOf(const Instance& in) {
-  RenderLuts r;
-  std::memset(&r, 0, sizeof(r));
-  r.c = in.c;
-  r.s = in.s;
-  r.T = in.T;
-  r.Tau = in.Tau;
-  r.S = in.S;
-  r.M = in.M;
-  r.I = in.I;
-  r.combined = in.combined;
-  for (int i = 0; i < 3; ++i) r.sky_k[i] = r.sun_k[i] = 1.0f;
-  return r;
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -1120,5 +1094,24 @@ atmo_status atmo_batch_save_luts(const atmo_batch* b, unsigned i, const char* di
   if (!b || i >= b->storages.size()) return Fail(ATMO_INVALID_ARG, "bad argument");
   if (!b->ran) return Fail(ATMO_NOT_READY, "atmo_batch_run has not been called");
   return SaveStorage(b->storages[i], directory, nullptr);
+}
+
+atmo_status atmo_lut_set_read(const atmo_lut_set* set, atmo_lut_kind kind, float* host_dst,
+                              size_t bytes) {
+  if (!set || !host_dst) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  const Shape& sh = set->luts.s;
+  const float4* src = nullptr;
+  size_t texels = 0;
+  switch (kind) {
+    case ATMO_LUT_TRANSMITTANCE: src = set->luts.T; texels = sh.t_texels(); break;
+    case ATMO_LUT_SCATTERING: src = set->luts.S; texels = (size_t)sh.s_texels(); break;
+    case ATMO_LUT_SINGLE_MIE: src = set->luts.M; texels = (size_t)sh.s_texels(); break;
+    case ATMO_LUT_IRRADIANCE: src = set->luts.I; texels = sh.i_texels(); break;
+    default: return Fail(ATMO_INVALID_ARG, "unknown LUT kind");
+  }
+  if (!src) return Fail(ATMO_INVALID_ARG, "no single-Mie texture with combined scattering textures");
+  if (bytes != texels * 16) return Fail(ATMO_INVALID_ARG, "host buffer size mismatch");
+  ATMO_CUDA_TRY(cudaMemcpy(host_dst, src, bytes, cudaMemcpyDeviceToHost));
+  return ATMO_OK;
 }
 }  // extern "C"

@@ -4,7 +4,9 @@
 
 #include <cuda_runtime.h>
 
-#include "atmo_device.cuh"
+#include <cstring>
+
+#include "atmo_instance.h"
 
 namespace atmo {
 
@@ -61,6 +63,32 @@ struct PinholeView {
 
 cudaError_t LaunchShadeView(const RenderLuts& luts, const PinholeView& v, cudaStream_t st);
 
+// The render view of one precomputed instance (luminance factors 1).
+inline RenderLuts LutsOf(const Instance& in) {
+  RenderLuts r;
+  std::memset(&r, 0, sizeof(r));
+  r.c = in.c;
+  r.s = in.s;
+  r.T = in.T;
+  r.Tau = in.Tau;
+  r.S = in.S;
+  r.M = in.M;
+  r.I = in.I;
+  r.combined = in.combined;
+  for (int i = 0; i < 3; ++i) r.sky_k[i] = r.sun_k[i] = 1.0f;
+  return r;
+}
+
 }  // namespace atmo
+
+// The C ABI's atmo_lut_set: a resident LUT set as the render-time queries
+// read it, with the API switches of its owner.
+struct atmo_lut_set {
+  atmo::RenderLuts luts;
+  bool radiance_api = true;    // RADIANCE_API_ENABLED (3 precomputed wavelengths)
+  bool luminance_api = true;   // *_SPECTRAL_RADIANCE_TO_LUMINANCE factors known
+  double solar[3] = {0, 0, 0};
+  double sun_angular_radius = 0;
+};
 
 #endif  // ATMO_RENDER_H_

@@ -1,0 +1,157 @@
+"""The serving engine (atmo_server_*): rebuilds batched at pass granularity
+with uneven LUT shapes and order counts, shading requests beside them, LUT
+sets resident under an HBM budget with LRU eviction.  Each result must be the
+same alone and in the mix (bit for bit: the kernels assign tiles per
+instance), and the same as the standalone batched precomputation."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import random_atmosphere
+
+HALF = (128, 32, 16, 64, 16, 4, 32, 8)
+SMALL = (64, 16, 4, 16, 8, 4, 16, 4)
+MEDIUM = (128, 32, 8, 32, 16, 8, 32, 8)
+LUTS = ("LUT_TRANSMITTANCE", "LUT_SCATTERING", "LUT_IRRADIANCE")
+
+
+def test_server_needs_a_device(atmo):
+    """Without a GPU the server reports the CUDA error instead of running."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(atmo.AtmoError) as e:
+        atmo.Server()
+    assert e.value.status == atmo.CUDA_ERROR
+
+
+def make_view(atmo, seed, width=96, height=54):
+    rng = np.random.default_rng(seed)
+    cam = rng.normal(size=3)
+    cam = cam / np.linalg.norm(cam) * (6360.0 + rng.uniform(0.0, 100.0))
+    fwd = rng.normal(size=3)
+    fwd /= np.linalg.norm(fwd)
+    tmp = rng.normal(size=3)
+    right = np.cross(fwd, tmp)
+    right /= np.linalg.norm(right)
+    up = np.cross(right, fwd)
+    sun = rng.normal(size=3)
+    sun /= np.linalg.norm(sun)
+    v = atmo.PinholeView()
+    for name, x in (("camera", cam), ("right", right), ("up", up), ("forward", fwd),
+                    ("sun_direction", sun), ("albedo", (0.1, 0.1, 0.1))):
+        setattr(v, name, (C.c_float * 3)(*x))
+    v.fov_y = np.radians(50.0)
+    v.width, v.height = width, height
+    depth = rng.uniform(0.1, 100.0, size=width * height).astype(np.float32)
+    return v, depth
+
+
+def shade(torch, server, set_id, view, depth):
+    d = torch.from_numpy(depth).cuda()
+    sky = torch.empty((view.height, view.width, 4), device="cuda")
+    shaded = torch.empty_like(sky)
+    t = server.submit_shade(set_id, view, d, sky, shaded)
+    return t, (d, sky, shaded)
+
+
+@pytest.mark.gpu
+def test_same_alone_and_in_the_mix(atmo, oracle, torch_cuda):
+    torch = torch_cuda
+    rng = np.random.default_rng(2024)
+    atms = [random_atmosphere(oracle, rng) for _ in range(7)]
+    atms.insert(3, oracle.earth_atmosphere())
+    shapes = [HALF, SMALL, MEDIUM, atmo.DEFAULT_SHAPE, SMALL, HALF, MEDIUM, SMALL]
+    orders = [2, 5, 3, 4, 6, 3, 2, 4]
+    key = 3   # the Earth set, compared alone and in the mix
+    view, depth = make_view(atmo, 1)
+
+    alone = atmo.Server()
+    t = alone.submit_rebuild(atms[key], shapes[key], orders[key])
+    alone.wait(t)
+    ref = {k: alone.lut_set(t).read(getattr(atmo, k)) for k in LUTS}
+    st, bufs = shade(torch, alone, t, view, depth)
+    alone.wait(st)
+    torch.cuda.synchronize()
+    ref_sky, ref_shaded = bufs[1].cpu().numpy(), bufs[2].cpu().numpy()
+    alone.close()
+
+    mix = atmo.Server(shade_streams=3)
+    tickets = []
+    keep = []
+    for i, (a, s, o) in enumerate(zip(atms, shapes, orders)):
+        tickets.append(mix.submit_rebuild(a, s, o))
+        if i >= 1:
+            # Shading on an earlier set while later rebuilds arrive.
+            v2, d2 = make_view(atmo, 100 + i)
+            keep.append(shade(torch, mix, tickets[i - 1], v2, d2))
+    key_shade, key_bufs = shade(torch, mix, tickets[key], view, depth)
+    for t in tickets:
+        mix.wait(t)
+    for t, _ in keep:
+        assert mix.wait(t).state == atmo.Server.DONE
+    mix.wait(key_shade)
+    torch.cuda.synchronize()
+    for k in LUTS:
+        np.testing.assert_array_equal(mix.lut_set(tickets[key]).read(getattr(atmo, k)), ref[k])
+    np.testing.assert_array_equal(key_bufs[1].cpu().numpy(), ref_sky)
+    np.testing.assert_array_equal(key_bufs[2].cpu().numpy(), ref_shaded)
+    stats = mix.stats()
+    assert stats.rounds > 0 and stats.kernels >= stats.rounds
+    # Some round launched a kernel for more than one instance.
+    assert stats.kernels < sum(4 + 3 * (o - 1) for o in orders)
+
+    # The same LUTs as the standalone batched precomputation.
+    b = atmo.Batch(atms[:3], shapes[:3], orders[:3])
+    b.run()
+    atmo.synchronize_stream()
+    for i in range(3):
+        for k in LUTS:
+            np.testing.assert_array_equal(mix.lut_set(tickets[i]).read(getattr(atmo, k)),
+                                          b.read(i, getattr(atmo, k)))
+    mix.close()
+
+
+@pytest.mark.gpu
+def test_budget_and_lru_eviction(atmo, oracle, torch_cuda):
+    torch = torch_cuda
+    # SMALL: final LUTs T 64x16 (twice, with the optical depth), I 16x4 and
+    # S 4x16x32 texels of 16 B; temporaries: delta irradiance, 3 delta S and
+    # the set-up tables (48 B rows, 16 B columns), each rounded up to 256 B.
+    final = 64 * 16 * 16 * 2 + 16 * 4 * 16 + 4 * 16 * 32 * 16
+    scratch = 16 * 4 * 16 + 3 * 4 * 16 * 32 * 16 + 4 * 16 * 48 + 256 + 4 * 16 * 48 + 256 + 256
+    # Room for two ready sets and a third being built (its final LUTs and
+    # temporaries), not for three ready sets and a fourth being built.
+    budget = int(3.5 * final) + scratch
+    srv = atmo.Server(hbm_budget_bytes=budget)
+    a = oracle.earth_atmosphere()
+    ids = []
+    for i in range(3):
+        ids.append(srv.submit_rebuild(a, SMALL, 2))
+        srv.wait(ids[-1])
+    srv.lut_set(ids[0])          # set 0 is now the most recently used
+    ids.append(srv.submit_rebuild(a, SMALL, 2))
+    srv.wait(ids[-1])
+    st = srv.stats()
+    assert st.evictions >= 1
+    srv.lut_set(ids[0])          # still resident
+    with pytest.raises(atmo.AtmoError) as e:
+        srv.lut_set(ids[1])      # the least recently used set went first
+    assert e.value.status == atmo.NOT_READY
+    # A shading request on an evicted set fails with NOT_READY.
+    view, depth = make_view(atmo, 3, 16, 8)
+    t, bufs = shade(torch, srv, ids[1], view, depth)
+    with pytest.raises(atmo.AtmoError) as e:
+        srv.wait(t)
+    assert e.value.status == atmo.NOT_READY
+    # A rebuild larger than the whole budget is refused.
+    big = srv.submit_rebuild(a, atmo.DEFAULT_SHAPE, 2)
+    with pytest.raises(atmo.AtmoError) as e:
+        srv.wait(big)
+    assert e.value.status == atmo.BUDGET
+    # Explicit eviction frees a ready set.
+    srv.evict(ids[0])
+    with pytest.raises(atmo.AtmoError):
+        srv.lut_set(ids[0])
+    srv.close()
