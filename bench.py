@@ -18,6 +18,12 @@ Reported (one JSON line on rank 0):
                  path's rebuilds/s,
   roofline       the scattering-density kernel against this GPU's FP32 FMA
                  throughput measured in the same run,
+  batched_mixed  256 seeded planets of uneven LUT shapes ({half, default,
+                 double-R}) and 2-6 orders in one batched pass sequence,
+  serving        a short seeded Poisson stream (2000 req/s, 10% rebuilds of
+                 such planets, 90% shading of 1920x1080 pinhole views with the
+                 three render functions) through atmo_server: p50/p99 latency
+                 per request type and throughput,
   cpu_baseline   the FP64 CPU oracle on a bounded sample, all host threads.
 
 --impl reference times the reference's CPU algorithm (the oracle port of
@@ -43,9 +49,14 @@ METRIC = "Earth LUT rebuilds/s batched vs plain on 1 GB300 @<=1e-3 vs FP64; p99 
 UNIT = "rebuilds/s"
 WORKLOAD = ("Earth atmosphere LUT rebuild, 256x64 / 256x128x32 / 64x16 RGBA FP32, "
             "4 scattering orders, 3 wavelengths, combined textures")
-# FP32 operations per density direction sample of the fast kernel's inner
-# loop (counted from the kernel's arithmetic, FMA = 2).
-DENSITY_FLOPS_PER_SAMPLE = 46.0
+# FP32 operations per direction sample of the fast scattering-density kernel
+# (FADD + FMUL + 2 x FFMA, counted by ncu's SASS op counters over one launch:
+# profiles/fast_kernels_earth_default_batch2.md): order 2 evaluates single
+# scattering with its phase functions, higher orders one radiance table.
+DENSITY_FLOPS_PER_SAMPLE = {2: 56.1, 3: 33.9}
+# DRAM bytes per density launch and instance, from the same capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance launch / 2).
+DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.22e6}
 
 
 def parse():
@@ -56,6 +67,9 @@ def parse():
     p.add_argument("--batch", type=int, default=16, help="atmospheres per batched step")
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-serving", action="store_true",
+                   help="skip the mixed-batch and serving measurements")
+    p.add_argument("--serving-seconds", type=float, default=3.0)
     return p.parse_args()
 
 
@@ -178,14 +192,10 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def earth_atmospheres(O, n):
-    return [O.earth_atmosphere() for _ in range(n)]
-
-
 def run_gpu(args):
     import torch
     import precomputed_atmospheric_scattering_gb300 as atmo
-    from oracle import oracle as O
+    from precomputed_atmospheric_scattering_gb300 import workloads as W
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
@@ -195,8 +205,8 @@ def run_gpu(args):
     atmo.build()
     atmo.lib()
     B = args.batch
-    shape = O.DEFAULT_SHAPE
-    atms = earth_atmospheres(O, B)
+    shape = W.DEFAULT
+    atms = [W.earth() for _ in range(B)]
     batch = atmo.Batch(atms, [shape] * B, 4, combined=True)
     kernels_per_step = batch.kernel_count()
     stream = torch.cuda.current_stream()
@@ -271,11 +281,17 @@ def run_gpu(args):
     lat.sort()
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
-    plain_ms = time_plain(atmo, O, torch, stream, args)
+    plain_ms = time_plain(atmo, W, torch, stream, args)
 
     # --- roofline of the scattering-density kernel ---------------------------
-    peak = density_roofline(atmo, O, torch, stream)
+    peak = atmo.measure_fp32_peak()
     roof = roofline_entry(batch, B, peak, stream)
+    del batch, single
+    torch.cuda.empty_cache()
+
+    # --- mixed batch (uneven shapes and order counts) and serving -----------
+    mixed = run_mixed_batch(atmo, W, torch, stream) if not args.no_serving else None
+    serving = run_serving(atmo, W, torch, args.serving_seconds) if not args.no_serving else None
 
     clk = clocks.summary()
     if rank != 0:
@@ -299,6 +315,10 @@ def run_gpu(args):
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clk,
     }
+    if mixed:
+        line["batched_mixed"] = mixed
+    if serving:
+        line["serving"] = serving
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_entry()
     print(json.dumps(line), flush=True)
@@ -306,14 +326,14 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-def time_plain(atmo, O, torch, stream, args):
+def time_plain(atmo, W, torch, stream, args):
     """One rebuild with the plain per-texel kernels (atmo_precompute, plain
     path) into device buffers, CUDA-event timed (median of 3)."""
-    s = atmo.LutShape(*O.DEFAULT_SHAPE)
+    s = atmo.LutShape(*W.DEFAULT)
     T = torch.zeros((64, 256, 4), device="cuda")
     S = torch.zeros((32, 128, 256, 4), device="cuda")
     I = torch.zeros((16, 64, 4), device="cuda")
-    atm = O.earth_atmosphere()
+    atm = W.earth()
     atmo.precompute(atm, s, 4, T, S, None, I, path=atmo.PATH_PLAIN, stream=stream)
     out = []
     for _ in range(3):
@@ -326,31 +346,153 @@ def time_plain(atmo, O, torch, stream, args):
     return sorted(out)[1]
 
 
-def density_roofline(atmo, O, torch, stream):
-    """The scattering-density kernel of one batched step against this GPU's
-    FP32 FMA throughput (measured here): launches timed with CUDA events on
-    the launching stream (a non-graph run of the same batch)."""
-    peak = atmo.measure_fp32_peak()
-    return peak
-
-
 def roofline_entry(batch, B, peak, stream):
     passes = batch.time_passes(stream)
-    dens = [ms for name, _, ms in passes if name == "scattering_density"]
+    dens = [(o, ms) for name, o, ms in passes if name == "scattering_density"]
     total = sum(ms for _, _, ms in passes)
     # One launch covers B instances x 1,048,576 texels x 512 directions.
     samples = B * 1048576 * 512
-    avg = sum(dens) / len(dens)
-    achieved = DENSITY_FLOPS_PER_SAMPLE * samples / (avg * 1e-3) / 1e12
+    flops = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
+    dens_ms = sum(ms for _, ms in dens)
+    achieved = flops / (dens_ms * 1e-3) / 1e12
+    traffic = sum(DENSITY_DRAM_BYTES_PER_INSTANCE[min(o, 3)] * B for o, _ in dens) / len(dens)
     return {"bound": "fp32", "kernel": "scattering density",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": None,
+            "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance "
+                              "launch per order (profiles/fast_kernels_earth_default_batch2.md), "
+                              "scaled to %d instances; bytes per launch, averaged over the "
+                              "step's density launches" % B,
             "peak_source": "FP32 FMA throughput measured in this run by atmo_measure_fp32_peak "
                            "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
-            "avg_launch_ms": avg, "launches_per_step": len(dens),
-            "share_of_step": sum(dens) / total, "flops_per_sample": DENSITY_FLOPS_PER_SAMPLE,
+            "avg_launch_ms": dens_ms / len(dens), "launches_per_step": len(dens),
+            "share_of_step": dens_ms / total,
+            "flops_per_sample": {str(k): v for k, v in DENSITY_FLOPS_PER_SAMPLE.items()},
             "passes_ms": {n + ("" if o == 0 else str(o)): round(ms, 4)
                           for n, o, ms in passes}}
+
+
+def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
+    """The batched configuration: n seeded planets with shapes from {half,
+    default, double-R} and 2-6 orders in one pass sequence (CUDA graph)."""
+    rng = np.random.default_rng(seed)
+    reqs = [W.random_rebuild(rng) for _ in range(n)]
+    b = atmo.Batch([a for a, _, _ in reqs], [s for _, s, _ in reqs], [o for _, _, o in reqs])
+    b.run(stream)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = sorted(times)[1]
+    out = {"instances": n, "ms": ms, "rebuilds_per_s": n / (ms * 1e-3),
+           "kernels_per_run": b.kernel_count(),
+           "shapes": {"half": sum(s == W.HALF for _, s, _ in reqs),
+                      "default": sum(s == W.DEFAULT for _, s, _ in reqs),
+                      "double_r": sum(s == W.DOUBLE_R for _, s, _ in reqs)},
+           "mean_orders": float(np.mean([o for _, _, o in reqs]))}
+    del b
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed=4,
+                pool=16):
+    """The serving configuration: a seeded Poisson stream of rebuild requests
+    (planets as in the batched configuration) and shading requests (the three
+    render functions over a 1920x1080 pinhole view, FOV 50 degrees) against
+    resident LUT sets, through atmo_server under a 120 GiB budget."""
+    rng = np.random.default_rng(seed)
+    srv = atmo.Server()
+    radius = {}
+    earth_id = srv.submit_rebuild(W.earth(), W.DEFAULT, 4)
+    srv.wait(earth_id)
+    radius[earth_id] = 6360.0
+    ready = [earth_id]
+    H, Wd = 1080, 1920
+    depth = torch.from_numpy(rng.uniform(0.1, 100.0, size=H * Wd).astype(np.float32)).cuda()
+    sky = [torch.empty((H, Wd, 4), device="cuda") for _ in range(pool)]
+    shaded = [torch.empty((H, Wd, 4), device="cuda") for _ in range(pool)]
+    slot_ticket = [None] * pool
+    # Warm-up shading (module load, first launches).
+    for j in range(4):
+        t = srv.submit_shade(earth_id, W.random_view(rng, 6360.0), depth, sky[j], shaded[j])
+        srv.wait(t)
+        srv.release_ticket(t)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.2) + 16))
+    arrivals = arrivals[arrivals < seconds]
+    building, records = [], []
+    nslot = 0
+    t0 = time.perf_counter()
+    for ta in arrivals:
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        if building:
+            # Newly built sets join the shading targets.
+            still = []
+            for tk in building:
+                if srv.poll(tk).state == atmo.Server.DONE:
+                    ready.append(tk)
+                else:
+                    still.append(tk)
+            building = still
+        if rng.random() < rebuild_fraction:
+            a, shape, orders = W.random_rebuild(rng)
+            tk = srv.submit_rebuild(a, shape, orders)
+            radius[tk] = a.bottom_radius
+            building.append(tk)
+            records.append(("rebuild", tk, time.perf_counter() - t0))
+        else:
+            set_id = ready[int(rng.integers(0, len(ready)))]
+            j = nslot % pool
+            nslot += 1
+            if slot_ticket[j] is not None:
+                srv.wait(slot_ticket[j], 120000)
+            tk = srv.submit_shade(set_id, W.random_view(rng, radius[set_id]), depth, sky[j],
+                                  shaded[j])
+            slot_ticket[j] = tk
+            records.append(("shade", tk, time.perf_counter() - t0))
+    submit_end = time.perf_counter() - t0
+    lat = {"rebuild": [], "shade": []}
+    end = 0.0
+    failed = 0
+    for kind, tk, ts in records:
+        try:
+            info = srv.wait(tk, 300000)
+        except atmo.AtmoError:
+            failed += 1
+            continue
+        lat[kind].append(info.latency_ms)
+        end = max(end, ts + info.latency_ms * 1e-3)
+    st = srv.stats()
+    srv.close()
+
+    def pct(xs, q):
+        xs = sorted(xs)
+        return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))] if xs else None
+
+    done = len(lat["rebuild"]) + len(lat["shade"])
+    return {
+        "offered_rate": rate, "seconds": seconds, "submitted": len(records),
+        "submit_seconds": submit_end, "completed": done, "failed": failed,
+        "throughput_req_per_s": done / end if end > 0 else None,
+        "rebuilds_per_s": len(lat["rebuild"]) / end if end > 0 else None,
+        "shades_per_s": len(lat["shade"]) / end if end > 0 else None,
+        "rebuild_ms": {"p50": pct(lat["rebuild"], 0.5), "p99": pct(lat["rebuild"], 0.99),
+                       "n": len(lat["rebuild"])},
+        "shade_ms": {"p50": pct(lat["shade"], 0.5), "p99": pct(lat["shade"], 0.99),
+                     "n": len(lat["shade"])},
+        "view": "1920x1080, FOV 50 deg: GetSkyRadiance, GetSkyRadianceToPoint and "
+                "GetSunAndSkyIrradiance per pixel",
+        "server": {"rounds": st.rounds, "kernels": st.kernels, "evictions": st.evictions,
+                   "resident_sets": st.resident_sets, "used_gb": st.used_bytes / 2 ** 30,
+                   "budget_gb": st.budget_bytes / 2 ** 30},
+    }
 
 
 def main():
