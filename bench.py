@@ -73,6 +73,21 @@ def parse():
     return p.parse_args()
 
 
+def replica_rate(local_seconds, local_units, world, device=None):
+    """Whole-job rate of independent replicas: the units every rank processed
+    over the slowest rank's time (max over ranks; no data-path collective,
+    only this reduction of the timings)."""
+    if world <= 1:
+        return local_units / local_seconds, local_seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([local_seconds, local_units], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t[1].item()) / float(mx[0].item()), float(mx[0].item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -228,12 +243,8 @@ def run_gpu(args):
             ev[k + 1].record(stream)
         barrier()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = B * args.steps * world / total_s
+    value, total_s = replica_rate(sum(step_ms) / 1000.0, B * args.steps, world,
+                                  device="cuda" if world > 1 else None)
 
     # --- end to end through the C API with host buffers ---------------------
     kinds = [atmo.LUT_TRANSMITTANCE, atmo.LUT_SCATTERING, atmo.LUT_IRRADIANCE]
@@ -263,8 +274,8 @@ def run_gpu(args):
     for _ in range(e2e_steps):
         e2e_step()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = B * e2e_steps * world / e2e_s
+    e2e_value, _ = replica_rate(time.perf_counter() - t0, B * e2e_steps, world,
+                                device="cuda" if world > 1 else None)
 
     # --- single-instance latency (fast) and the plain path ------------------
     single = atmo.Batch([atms[0]], [shape], 4, combined=True)

@@ -163,8 +163,10 @@ const char* atmo_last_error(void);
 atmo_status atmo_synchronize(atmo_stream stream);
 
 /* ---- Model (atmosphere/model.h) ------------------------------------------- */
-/* Validates and converts the parameters like atmosphere/model.cc:613-745 and
-   allocates the final LUTs on the current CUDA device.  shape may be NULL. */
+/* Validates and converts the parameters like atmosphere/model.cc:613-745.
+   Device memory is allocated by the first atmo_model_init, LUT request or
+   atmo_model_load_luts, on the CUDA device current then.  shape may be NULL
+   (the reference's sizes). */
 atmo_status atmo_model_create(const atmo_model_params* params, const atmo_lut_shape* shape,
                               atmo_model** out);
 atmo_status atmo_model_destroy(atmo_model* model);
