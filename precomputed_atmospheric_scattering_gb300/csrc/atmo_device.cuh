@@ -571,6 +571,7 @@ ATMO_HD void SplitTexel(const Shape& s, long long idx, int* k, int* j, int* c, i
 // direction of functions.glsl:1176-1180 (omega_s = (sx, sy, mu_s)).
 struct TexelAngles {
   float mu, mu_s, nu, omega_x, sx, sy;
+  bool on_node;   // nu not clamped: the texel's own nu node (functions.glsl:924-925)
 };
 ATMO_HD TexelAngles MakeAngles(const Shape& s, const TexelRow& row, const TexelCol& col,
                                int n) {
@@ -582,6 +583,7 @@ ATMO_HD TexelAngles MakeAngles(const Shape& s, const TexelRow& row, const TexelC
   float mm = row.mu * col.mu_s;
   float lim = row.omega_x * col.sin_s;   // sqrt((1 - mu^2)(1 - mu_s^2))
   float t = clampf(nu_g - mm, -lim, lim);
+  a.on_node = t == nu_g - mm;
   a.nu = mm + t;
   a.sx = row.omega_x == 0.0f ? 0.0f : clampf(t / row.omega_x, -col.sin_s, col.sin_s);
   float ax = fabsf(a.sx);

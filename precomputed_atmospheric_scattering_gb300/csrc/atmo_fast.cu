@@ -24,21 +24,21 @@ constexpr int kDensityFastThreads = 256;
 
 int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
 
-// Piecewise-linear functions staged in shared memory are stored per node as
-// the midpoint of the segment to the next node and the segment's slope (the
-// slope is 0 at the last node), so that a lookup is mid + w slope with w in
-// [-0.5, 0.5].  The segment is found by rounding rather than flooring: adding
-// 1.5 x 2^23 to x (|x| < 2^22) leaves round(x) in the sum's low mantissa bits,
-// ties to even, and (sum - 1.5 x 2^23) is round(x) as a float, exactly.  With
-// x = node coordinate - 0.5 >= -0.5 that selects the segment [n, n + 1]
-// holding the coordinate (a coordinate on a node may take either segment;
-// both give the node's value).  The sum's bit pattern, times the entry size,
-// plus a row offset that cancels the constant's exponent bits (mod 2^32), is
-// the entry's shared-memory address.
+// Piecewise-linear functions staged in shared memory are stored per segment
+// [n, n + 1] as the line a + b x of the segment in the coordinate x = node
+// coordinate - 0.5 (b = the slope to the next node, 0 at the last node; a =
+// L[n] + b (0.5 - n)), so a lookup is one FMA per channel.  The segment is
+// found by rounding rather than flooring: adding 1.5 x 2^23 to x (|x| < 2^22)
+// leaves round(x) in the sum's low mantissa bits, ties to even.  With x >= -0.5
+// that selects the segment holding the coordinate (a coordinate on a node may
+// take either segment; both give the node's value).  The sum's bit pattern,
+// times the entry size, plus a row offset that cancels the constant's exponent
+// bits (mod 2^32), is the entry's shared-memory address.  The intercept's
+// cancellation costs at most ~n ulp of the node values (n < 128).
 constexpr float kRoundMagic = 12582912.0f;
 constexpr uint32_t kRoundMagicBits = 0x4B400000u;
 
-// One node entry: mid.xyz, slope.x | slope.y, slope.z, -, -.
+// One segment entry: a.xyz, b.x | b.y, b.z, -, -.
 constexpr int kNodeBytes = 32;
 
 template <int kOffset>
@@ -55,21 +55,23 @@ __device__ __forceinline__ float2 LoadShared2(uint32_t addr) {
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(kOffset));
   return v;
 }
-__device__ __forceinline__ void StoreNode(float4* entry, float4 v, float4 next) {
+// Segment n of a row: node values v = L[n], next = L[n + 1] (next = v at the
+// last node).
+__device__ __forceinline__ void StoreSegment(float4* entry, float4 v, float4 next, int n) {
   const float dx = next.x - v.x, dy = next.y - v.y, dz = next.z - v.z;
-  entry[0] = make_float4(fmaf(0.5f, dx, v.x), fmaf(0.5f, dy, v.y), fmaf(0.5f, dz, v.z), dx);
+  const float c = 0.5f - float(n);
+  entry[0] = make_float4(fmaf(c, dx, v.x), fmaf(c, dy, v.y), fmaf(c, dz, v.z), dx);
   entry[1] = make_float4(dy, dz, 0.0f, 0.0f);
 }
-// The staged function at node coordinate u + 0.5 (u >= -0.5) of the table
-// whose entries (kStride bytes apart, the function's at byte kOffset) start
-// at row_adj + kRoundMagicBits kStride.
+// The staged function at x = node coordinate - 0.5 (x >= -0.5), t = x + 1.5 x
+// 2^23, of the table whose entries (kStride bytes apart, the function's at
+// byte kOffset) start at row_adj + kRoundMagicBits kStride.
 template <int kStride, int kOffset>
-__device__ __forceinline__ F3 EvalNodes(float u, float t, uint32_t row_adj) {
-  const float w = u - (t - kRoundMagic);
+__device__ __forceinline__ F3 EvalNodes(float x, float t, uint32_t row_adj) {
   const uint32_t a = (uint32_t)__float_as_int(t) * (uint32_t)kStride + row_adj;
   const float4 p = LoadShared4<kOffset>(a);
   const float2 q = LoadShared2<kOffset + 16>(a);
-  return F3{fmaf(w, p.w, p.x), fmaf(w, q.x, p.y), fmaf(w, q.y, p.z)};
+  return F3{fmaf(x, p.w, p.x), fmaf(x, q.x, p.y), fmaf(x, q.y, p.z)};
 }
 __host__ __device__ constexpr uint32_t RowAdjust(uint32_t base, int stride) {
   return base - kRoundMagicBits * (uint32_t)stride;
@@ -198,11 +200,12 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   for (int e = threadIdx.x; e < staged; e += blockDim.x) {
     if (e < kSpecies * nodes) {
       const int sp = e / nodes, ne = e - sp * nodes;
-      const bool last = (ne % NU) == NU - 1;
-      StoreNode(E + (ne * kSpecies + sp) * (kNodeBytes / 16), V[e], last ? V[e] : V[e + 1]);
+      const int n = ne % NU;
+      StoreSegment(E + (ne * kSpecies + sp) * (kNodeBytes / 16), V[e],
+                   n == NU - 1 ? V[e] : V[e + 1], n);
     } else {
       const int i = e - kSpecies * nodes;
-      StoreNode(G + i * (kNodeBytes / 16), V[e], i == s.iw - 1 ? V[e] : V[e + 1]);
+      StoreSegment(G + i * (kNodeBytes / 16), V[e], i == s.iw - 1 ? V[e] : V[e + 1], i);
     }
   }
   __syncthreads();
@@ -421,9 +424,12 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
       const TexelAngles ang = MakeAngles(s, row, in.tab.cols[col], n);
       rmu_s[m] = row.r * ang.mu_s;
       nu[m] = ang.nu;
+      // A texel whose nu is not clamped sits on its own nu node n: the
+      // reference's FP64 coordinate (nu + 1) / 2 (NU - 1) is n to ~1e-16, so
+      // the neighbouring node's weight is taken as 0 and its taps skipped.
       const float tex_coord_x = (ang.nu + 1.0f) * 0.5f * float(s.snu - 1);
-      const float tex_x = floorf(tex_coord_x);
-      lnu[m] = tex_coord_x - tex_x;
+      const float tex_x = ang.on_node ? float(n) : floorf(tex_coord_x);
+      lnu[m] = ang.on_node ? 0.0f : tex_coord_x - tex_x;
       xb[m] = tex_x * smus_f - 0.5f;
       acc[m] = f3(0.0f);
     }
@@ -470,11 +476,16 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
           const int c0 = min(max(i0, 0), nmax), c1 = min(max(i0 + 1, 0), nmax);
           const int c2 = min(max(i0 + s.smus, 0), nmax), c3 = min(max(i0 + s.smus + 1, 0), nmax);
           const float l1 = lnu[m], l0 = 1.0f - l1;
-          const float v0 = (1.0f - a) * l0, v1 = a * l0, v2 = (1.0f - a) * l1, v3 = a * l1;
-          const float4 t0 = L[c0], t1 = L[c1], t2 = L[c2], t3 = L[c3];
-          const F3 S{fmaf(t3.x, v3, fmaf(t2.x, v2, fmaf(t1.x, v1, t0.x * v0))),
-                     fmaf(t3.y, v3, fmaf(t2.y, v2, fmaf(t1.y, v1, t0.y * v0))),
-                     fmaf(t3.z, v3, fmaf(t2.z, v2, fmaf(t1.z, v1, t0.z * v0)))};
+          const float v0 = (1.0f - a) * l0, v1 = a * l0;
+          const float4 t0 = L[c0], t1 = L[c1];
+          F3 S{fmaf(t1.x, v1, t0.x * v0), fmaf(t1.y, v1, t0.y * v0),
+               fmaf(t1.z, v1, t0.z * v0)};
+          if (l1 != 0.0f) {
+            const float v2 = (1.0f - a) * l1, v3 = a * l1;
+            const float4 t2 = L[c2], t3 = L[c3];
+            S = F3{fmaf(t3.x, v3, fmaf(t2.x, v2, S.x)), fmaf(t3.y, v3, fmaf(t2.y, v2, S.y)),
+                   fmaf(t3.z, v3, fmaf(t2.z, v2, S.z))};
+          }
           acc[m] = fma3(S, F3{sm.tx, sm.ty, sm.tz}, acc[m]);
         }
       }
