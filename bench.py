@@ -222,6 +222,8 @@ def run_gpu(args):
     B = args.batch
     shape = W.DEFAULT
     atms = [W.earth() for _ in range(B)]
+    # Block shapes of the row-restructured kernels, timed on this GPU.
+    tuning = atmo.autotune(atms[0], shape, 4).as_dict()
     batch = atmo.Batch(atms, [shape] * B, 4, combined=True)
     kernels_per_step = batch.kernel_count()
     stream = torch.cuda.current_stream()
@@ -313,7 +315,8 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: Earth parameters of the reference demo (no dataset)",
         "config": {"workload": WORKLOAD, "batch": B, "orders": 4,
-                   "lut_shape": list(shape), "parallelism": "replicas (independent batches "
+                   "lut_shape": list(shape), "tuning": tuning,
+                   "parallelism": "replicas (independent batches "
                    "per GPU)" if world > 1 else "single GPU",
                    "l2": "no flush: each step's working set (%d MB) exceeds the 129 MB L2"
                          % (B * 64)},
@@ -388,6 +391,9 @@ def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
     default, double-R} and 2-6 orders in one pass sequence (CUDA graph)."""
     rng = np.random.default_rng(seed)
     reqs = [W.random_rebuild(rng) for _ in range(n)]
+    tunings = {name: atmo.autotune(W.earth(), shape, 4).as_dict()
+               for name, shape in (("half", W.HALF), ("default", W.DEFAULT),
+                                   ("double_r", W.DOUBLE_R))}
     b = atmo.Batch([a for a, _, _ in reqs], [s for _, s, _ in reqs], [o for _, _, o in reqs])
     b.run(stream)
     torch.cuda.synchronize()
@@ -405,7 +411,7 @@ def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
            "shapes": {"half": sum(s == W.HALF for _, s, _ in reqs),
                       "default": sum(s == W.DEFAULT for _, s, _ in reqs),
                       "double_r": sum(s == W.DOUBLE_R for _, s, _ in reqs)},
-           "mean_orders": float(np.mean([o for _, _, o in reqs]))}
+           "mean_orders": float(np.mean([o for _, _, o in reqs])), "tunings": tunings}
     del b
     torch.cuda.empty_cache()
     return out

@@ -402,6 +402,26 @@ atmo_status atmo_server_lut_set(atmo_server* server, uint64_t set_id, const atmo
 /* Frees a ready, idle set now. */
 atmo_status atmo_server_evict(atmo_server* server, uint64_t set_id);
 atmo_status atmo_server_get_stats(atmo_server* server, atmo_server_stats* out);
+/* ---- autotuner --------------------------------------------------------------- */
+/* Block shape of the row-restructured single- and multiple-scattering kernels
+   for one LUT shape: scattering-LUT rows per block and ray samples per
+   shared-memory line stage (0, 0: the built-in choice).  A tuning changes
+   only how work is grouped: every LUT is bit-identical under every tuning. */
+typedef struct {
+  int multiple_rows, multiple_group;
+  int single_rows, single_group;
+  float multiple_ms, single_ms;   /* atmo_autotune: best time per instance of each kernel */
+} atmo_tuning;
+/* Times every launchable block shape on this GPU for `shape` (a batch of
+   `instances` copies of `atmosphere`, 0: 4) and registers the fastest for
+   every model, batch and server instance of that shape created afterwards
+   in this process.  Synchronous. */
+atmo_status atmo_autotune(const atmo_atmosphere* atmosphere, const atmo_lut_shape* shape,
+                          unsigned instances, atmo_tuning* out);
+/* Registers a tuning for `shape` (checked for launchability); NULL restores
+   the built-in choice.  Host only. */
+atmo_status atmo_set_tuning(const atmo_lut_shape* shape, const atmo_tuning* tuning);
+atmo_status atmo_get_tuning(const atmo_lut_shape* shape, atmo_tuning* out);
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Measures this GPU's FP32 FMA throughput (TFLOP/s, 2 FLOP per FMA) with a
    short dependent-chain kernel over every SM: the denominator of the

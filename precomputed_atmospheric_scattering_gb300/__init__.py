@@ -128,6 +128,16 @@ class PinholeView(C.Structure):
                 ("sun_direction", _F3), ("albedo", _F3)]
 
 
+class Tuning(C.Structure):
+    """atmo_tuning: block shape of the row-restructured kernels for one LUT shape."""
+    _fields_ = [("multiple_rows", C.c_int), ("multiple_group", C.c_int),
+                ("single_rows", C.c_int), ("single_group", C.c_int),
+                ("multiple_ms", C.c_float), ("single_ms", C.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_rebuilds_in_flight", C.c_uint),
                 ("shade_streams", C.c_uint), ("combined", C.c_int)]
@@ -228,6 +238,9 @@ def lib():
             "atmo_server_lut_set": [vp, C.c_uint64, P(vp)],
             "atmo_server_evict": [vp, C.c_uint64],
             "atmo_server_get_stats": [vp, P(ServerStats)],
+            "atmo_autotune": [P(Atmosphere), P(LutShape), C.c_uint, P(Tuning)],
+            "atmo_set_tuning": [P(LutShape), P(Tuning)],
+            "atmo_get_tuning": [P(LutShape), P(Tuning)],
             "atmo_model_save_luts": [vp, C.c_char_p],
             "atmo_model_load_luts": [vp, C.c_char_p],
             "atmo_batch_save_luts": [vp, C.c_uint, C.c_char_p],
@@ -597,6 +610,30 @@ class Server:
         s = ServerStats()
         _check(lib().atmo_server_get_stats(self._h, C.byref(s)))
         return s
+
+
+def autotune(atmosphere, shape=None, instances=4) -> Tuning:
+    """Times the launchable block shapes of the single- and multiple-scattering
+    kernels for `shape` on this GPU and registers the fastest (results are
+    bit-identical under every tuning)."""
+    t = Tuning()
+    s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+    _check(lib().atmo_autotune(C.byref(Atmosphere.from_buffer_of(atmosphere)), C.byref(s),
+                               instances, C.byref(t)))
+    return t
+
+
+def set_tuning(shape, tuning=None):
+    """Registers (or, with None, clears) a tuning for a LUT shape."""
+    s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+    _check(lib().atmo_set_tuning(C.byref(s), C.byref(tuning) if tuning is not None else None))
+
+
+def get_tuning(shape=None) -> Tuning:
+    t = Tuning()
+    s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+    _check(lib().atmo_get_tuning(C.byref(s), C.byref(t)))
+    return t
 
 
 def measure_fp32_peak():

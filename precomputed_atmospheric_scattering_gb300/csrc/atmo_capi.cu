@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -1112,6 +1113,144 @@ atmo_status atmo_lut_set_read(const atmo_lut_set* set, atmo_lut_kind kind, float
   if (!src) return Fail(ATMO_INVALID_ARG, "no single-Mie texture with combined scattering textures");
   if (bytes != texels * 16) return Fail(ATMO_INVALID_ARG, "host buffer size mismatch");
   ATMO_CUDA_TRY(cudaMemcpy(host_dst, src, bytes, cudaMemcpyDeviceToHost));
+  return ATMO_OK;
+}
+
+// ---- autotuner ---------------------------------------------------------------
+atmo_status atmo_set_tuning(const atmo_lut_shape* shape, const atmo_tuning* tuning) {
+  atmo_lut_shape ls = shape ? *shape : DefaultShape();
+  std::string why;
+  if (!ValidShape(ls, &why)) return Fail(ATMO_INVALID_ARG, why);
+  if (!tuning) {
+    SetTuning(ls, nullptr);
+    return ATMO_OK;
+  }
+  SetTuning(ls, nullptr);
+  const Shape s = ToShape(ls);
+  const bool m_default = tuning->multiple_rows == 0 && tuning->multiple_group == 0;
+  const bool s_default = tuning->single_rows == 0 && tuning->single_group == 0;
+  if ((!m_default && !FastTuningValid(s, false, tuning->multiple_rows, tuning->multiple_group)) ||
+      (!s_default && !FastTuningValid(s, true, tuning->single_rows, tuning->single_group)))
+    return Fail(ATMO_INVALID_ARG,
+                "block shape not launchable for this LUT shape (rows 1-4 with rows x NU x "
+                "MU_S <= 256, samples per stage 1-8, shared memory <= 48 KB)");
+  const int t[4] = {tuning->multiple_rows, tuning->multiple_group, tuning->single_rows,
+                    tuning->single_group};
+  SetTuning(ls, t);
+  return ATMO_OK;
+}
+
+atmo_status atmo_get_tuning(const atmo_lut_shape* shape, atmo_tuning* out) {
+  if (!out) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  atmo_lut_shape ls = shape ? *shape : DefaultShape();
+  std::string why;
+  if (!ValidShape(ls, &why)) return Fail(ATMO_INVALID_ARG, why);
+  const Shape s = ToShape(ls);
+  out->multiple_rows = s.tune[0];
+  out->multiple_group = s.tune[1];
+  out->single_rows = s.tune[2];
+  out->single_group = s.tune[3];
+  return ATMO_OK;
+}
+
+atmo_status atmo_autotune(const atmo_atmosphere* atmosphere, const atmo_lut_shape* shape,
+                          unsigned instances, atmo_tuning* out) {
+  if (!atmosphere || !out) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  atmo_lut_shape ls = shape ? *shape : DefaultShape();
+  std::string why;
+  if (!ValidShape(ls, &why) || !ValidAtmosphere(*atmosphere, &why))
+    return Fail(ATMO_INVALID_ARG, why);
+  const unsigned n = instances ? instances : 4;
+  if (n > 64) return Fail(ATMO_INVALID_ARG, "instances must be <= 64");
+  SetTuning(ls, nullptr);
+  const Shape base = ToShape(ls);
+  std::vector<Storage> storages(n);
+  for (unsigned i = 0; i < n; ++i) {
+    atmo_status st = storages[i].Allocate(base, true, false);
+    if (st != ATMO_OK) {
+      for (auto& x : storages) x.Free();
+      return st;
+    }
+  }
+  struct Trial {
+    int rows, group;
+    float single_ms, multiple_ms;
+  };
+  std::vector<Trial> trials;
+  const int rows_c[3] = {1, 2, 4}, group_c[6] = {1, 2, 3, 4, 6, 8};
+  for (int r : rows_c) {
+    for (int g : group_c) {
+      const bool ms_ok = FastTuningValid(base, false, r, g);
+      const bool ss_ok = FastTuningValid(base, true, r, g);
+      if (!ms_ok && !ss_ok) continue;
+      Shape s = base;
+      s.tune[0] = ms_ok ? r : 0;
+      s.tune[1] = ms_ok ? g : 0;
+      s.tune[2] = ss_ok ? r : 0;
+      s.tune[3] = ss_ok ? g : 0;
+      Program prog;
+      prog.path = ATMO_PATH_FAST;
+      std::vector<int> members;
+      for (unsigned i = 0; i < n; ++i) {
+        const Storage& sto = storages[i];
+        Instance in;
+        std::memset(&in, 0, sizeof(in));
+        in.c = MakeConsts(*atmosphere, nullptr);
+        in.s = s;
+        in.tab = sto.tab;
+        in.T = sto.T;
+        in.Tau = sto.Tau;
+        in.I = sto.I;
+        in.dI = sto.dI;
+        in.dR = sto.dR;
+        in.dM = sto.dM;
+        in.dJ = sto.dJ;
+        in.S = sto.S;
+        in.combined = 1;
+        prog.slots.push_back(in);
+        prog.orders.push_back(2);
+        members.push_back((int)i);
+      }
+      prog.AddStage(members);
+      Trial t{r, g, 1e30f, 1e30f};
+      for (int rep = 0; rep < 3; ++rep) {
+        std::vector<float> ms;
+        atmo_status st = prog.TimeSteps(nullptr, &ms);
+        if (st != ATMO_OK) {
+          for (auto& x : storages) x.Free();
+          return st;
+        }
+        float single = 0.0f, multiple = 0.0f;
+        for (size_t i = 0; i < prog.steps().size(); ++i) {
+          if (prog.steps()[i].pass == Pass::kSingle) single += ms[i];
+          if (prog.steps()[i].pass == Pass::kMultiple) multiple += ms[i];
+        }
+        if (ss_ok) t.single_ms = std::min(t.single_ms, single);
+        if (ms_ok) t.multiple_ms = std::min(t.multiple_ms, multiple);
+      }
+      trials.push_back(t);
+    }
+  }
+  for (auto& x : storages) x.Free();
+  atmo_tuning best{0, 0, 0, 0, 0.0f, 0.0f};
+  float best_s = 1e30f, best_m = 1e30f;
+  for (const Trial& t : trials) {
+    if (t.multiple_ms < best_m) {
+      best_m = t.multiple_ms;
+      best.multiple_rows = t.rows;
+      best.multiple_group = t.group;
+    }
+    if (t.single_ms < best_s) {
+      best_s = t.single_ms;
+      best.single_rows = t.rows;
+      best.single_group = t.group;
+    }
+  }
+  best.multiple_ms = best_m / (float)n;
+  best.single_ms = best_s / (float)n;
+  const int tv[4] = {best.multiple_rows, best.multiple_group, best.single_rows, best.single_group};
+  SetTuning(ls, tv);
+  *out = best;
   return ATMO_OK;
 }
 }  // extern "C"

@@ -51,6 +51,9 @@ inline atmo_lut_shape DefaultShape() {
   return s;
 }
 
+// Fills the tuned block shapes registered for these LUT sizes (atmo_program.cu).
+void ApplyTuning(const atmo_lut_shape& sizes, Shape* s);
+
 inline Shape ToShape(const atmo_lut_shape& s) {
   Shape t;
   t.tw = s.transmittance_width;
@@ -67,6 +70,8 @@ inline Shape ToShape(const atmo_lut_shape& s) {
     t.map_c0[i] = 0.5f / fn;
     t.map_c1[i] = 1.0f - 1.0f / fn;
   }
+  for (int i = 0; i < 4; ++i) t.tune[i] = 0;
+  ApplyTuning(s, &t);
   return t;
 }
 

@@ -110,6 +110,11 @@ struct Shape {
   int iw, ih;             // irradiance W x H
   float map_c0[kMapCount];  // 0.5 / n (IEEE, as the kernels would compute it)
   float map_c1[kMapCount];  // 1 - 1 / n
+  // Block shape of the row-restructured kernels (0: the built-in choice):
+  // multiple-scattering rows per block and samples per line stage, then the
+  // same for single scattering.  Set by the autotuner; results do not depend
+  // on it.
+  int tune[4];
   ATMO_HD int sw() const { return snu * smus; }
   ATMO_HD long long s_texels() const { return (long long)snu * smus * smu * sr; }
   ATMO_HD int t_texels() const { return tw * th; }

@@ -312,13 +312,17 @@ struct MultipleFastDims {
   int rows;    // LUT rows per block
   int group;   // samples per line stage
 };
+// Rows per block and samples per line stage: the tuned values of the shape,
+// else as many rows (up to 4) as fill 256 threads and two line buffers of
+// group x rows x W float4 within 32 KB.
 __host__ __device__ inline MultipleFastDims MultipleDims(const Shape& s) {
   const int W = s.sw();
   int rows = kMultipleFastThreads / W;
   rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
-  // Two line buffers of group x rows x W float4 within 32 KB.
+  if (s.tune[0] > 0) rows = s.tune[0];
   int group = 32768 / (2 * 16 * rows * W);
   group = group < 1 ? 1 : (group > 4 ? 4 : group);
+  if (s.tune[1] > 0) group = s.tune[1];
   return MultipleFastDims{rows, group};
 }
 bool MultipleFastFits(const Shape& s) {
@@ -552,8 +556,10 @@ struct __align__(16) SunSample {
 __host__ __device__ inline MultipleFastDims SingleDims(const Shape& s) {
   int rows = kMultipleFastThreads / s.sw();
   rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
+  if (s.tune[2] > 0) rows = s.tune[2];
   int group = 32768 / (2 * 16 * rows * s.tw);
   group = group < 1 ? 1 : (group > 4 ? 4 : group);
+  if (s.tune[3] > 0) group = s.tune[3];
   return MultipleFastDims{rows, group};
 }
 int SingleFastSmem(const Shape& s) {
@@ -566,6 +572,20 @@ bool SingleFastFits(const Shape& s) {
 int SingleFastTiles(const Shape& s) {
   const int rows = SingleDims(s).rows;
   return (s.sr * s.smu + rows - 1) / rows;
+}
+
+// Whether a (rows, group) block shape is launchable for shape s: one texel
+// column per thread needs rows x W <= 256 (wider rows take one row per
+// block), and the shared memory must stay within 48 KB.
+bool FastTuningValid(const Shape& s, bool single, int rows, int group) {
+  if (rows < 1 || rows > 4 || group < 1 || group > 8) return false;
+  const int W = s.sw();
+  if (W > kMultipleFastThreads * kMultipleFastMaxCols) return false;
+  if (rows > 1 && rows * W > kMultipleFastThreads) return false;
+  Shape t = s;
+  t.tune[single ? 2 : 0] = rows;
+  t.tune[single ? 3 : 1] = group;
+  return (single ? SingleFastSmem(t) : MultipleFastSmem(t)) <= 48 * 1024;
 }
 
 // Sample i of the ray of LUT row `rowi` (the per-sample part of

@@ -33,6 +33,9 @@ int SingleFastTiles(const Shape& s);
 int SingleFastSmem(const Shape& s);
 cudaError_t LaunchSingleFast(const Instance* insts, WorkList wl, int tiles, int smem_bytes,
                              cudaStream_t st);
+// A (rows per block, samples per line stage) tuning of the single (single =
+// true) or multiple scattering kernel that can run for shape s.
+bool FastTuningValid(const Shape& s, bool single, int rows, int group);
 // The row-restructured multiple-scattering kernel needs W = NU x MU_S <= 1024.
 bool MultipleFastFits(const Shape& s);
 int MultipleFastTiles(const Shape& s);

@@ -1,7 +1,12 @@
 // atmo_program.cu -- device storage and launch programs (see atmo_program.h).
 #include "atmo_program.h"
 
+#include <array>
+
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "atmo_kernels.h"
 #include "atmo_tables.cuh"
@@ -10,7 +15,34 @@ namespace atmo {
 
 namespace {
 thread_local std::string g_last_error = "no error";
+
+// Tuned block shapes by LUT sizes, for this process.
+using SizeKey = std::tuple<int, int, int, int, int, int, int, int>;
+std::mutex g_tuning_mutex;
+std::map<SizeKey, std::array<int, 4>> g_tuning;
+
+SizeKey KeyOf(const atmo_lut_shape& s) {
+  return SizeKey(s.transmittance_width, s.transmittance_height, s.scattering_r,
+                 s.scattering_mu, s.scattering_mu_s, s.scattering_nu, s.irradiance_width,
+                 s.irradiance_height);
+}
 }  // namespace
+
+void ApplyTuning(const atmo_lut_shape& sizes, Shape* s) {
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  auto it = g_tuning.find(KeyOf(sizes));
+  if (it == g_tuning.end()) return;
+  for (int i = 0; i < 4; ++i) s->tune[i] = it->second[i];
+}
+
+void SetTuning(const atmo_lut_shape& sizes, const int* tune) {
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  if (!tune) {
+    g_tuning.erase(KeyOf(sizes));
+    return;
+  }
+  g_tuning[KeyOf(sizes)] = {tune[0], tune[1], tune[2], tune[3]};
+}
 
 void SetError(const std::string& msg) { g_last_error = msg; }
 const char* LastError() { return g_last_error.c_str(); }

@@ -14,6 +14,11 @@
 
 namespace atmo {
 
+// Registers the tuned block shapes (4 values, see Shape::tune) for LUTs of
+// these sizes in this process; NULL removes them.  Shapes made afterwards by
+// ToShape carry them.
+void SetTuning(const atmo_lut_shape& sizes, const int* tune);
+
 // Last error message of this host thread.
 void SetError(const std::string& msg);
 atmo_status CudaFail(cudaError_t e, const char* what);
