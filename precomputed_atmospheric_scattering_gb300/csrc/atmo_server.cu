@@ -211,10 +211,15 @@ struct atmo_server {
 
 atmo_status atmo_server::Init() {
   ATMO_CUDA_TRY(cudaGetDevice(&device));
-  ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&build_stream, cudaStreamNonBlocking));
+  // Rebuild rounds get the highest stream priority: their blocks are
+  // scheduled ahead of pending shading blocks, so a rebuild's many small
+  // rounds are not each queued behind a full-screen shading request.
+  int least = 0, greatest = 0;
+  ATMO_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  ATMO_CUDA_TRY(cudaStreamCreateWithPriority(&build_stream, cudaStreamNonBlocking, greatest));
   for (unsigned i = 0; i < cfg.shade_streams; ++i) {
     cudaStream_t st;
-    ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    ATMO_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, least));
     shade_streams.push_back(st);
   }
   cudaMemPoolProps props;

@@ -155,3 +155,22 @@ def test_budget_and_lru_eviction(atmo, oracle, torch_cuda):
     with pytest.raises(atmo.AtmoError):
         srv.lut_set(ids[0])
     srv.close()
+
+
+@pytest.mark.gpu
+def test_destroy_with_work_in_flight(atmo, oracle, torch_cuda):
+    """Closing the server while rebuilds and shading requests run returns
+    once their GPU work has finished (no hang, no fault)."""
+    torch = torch_cuda
+    import time
+    srv = atmo.Server()
+    rng = np.random.default_rng(9)
+    ids = [srv.submit_rebuild(random_atmosphere(oracle, rng), MEDIUM, 4) for _ in range(6)]
+    keep = []
+    view, depth = make_view(atmo, 4)
+    for t in ids[:3]:
+        keep.append(shade(torch, srv, t, view, depth))
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 60.0
+    torch.cuda.synchronize()
