@@ -123,7 +123,9 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
       const float dl = task.sys[q] * cs.y;
       const float bu = fmaf(base, half_nu, nu_off);
       const float bg = kGround ? fmaf(base, g_scale, g_off) : 0.0f;
-      F3 Ls = f3(0.0f);
+      // Ls is seeded with the first side's radiance (an explicit 0 + x
+      // would cost an add per channel: IEEE keeps it).
+      F3 Ls;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         const float sdl = side == 0 ? dl : -dl;
@@ -137,9 +139,11 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
           const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
           const float nu1 = base + sdl;
           const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
-          Ls = fma3(fma3(M, r1 * r1 * r1, L), fmaf(nu1, nu1, 1.0f), Ls);
+          const F3 L1 = fma3(M, r1 * r1 * r1, L);
+          const float q1 = fmaf(nu1, nu1, 1.0f);
+          Ls = side == 0 ? L1 * q1 : fma3(L1, q1, Ls);
         } else {
-          Ls += L;
+          Ls = side == 0 ? L : Ls + L;
         }
         if (kGround) {
           // Ground bounce: the ground point is at radius Rb, so the cosine
