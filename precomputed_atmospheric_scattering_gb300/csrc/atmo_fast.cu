@@ -93,12 +93,18 @@ int DensityFastSmem(const Shape& s, int order) {
 constexpr int kDensityTexelsPerTask = 2;
 
 struct DensityTask {
-  float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];   // sx, sy x sin(theta_l)
+  // sx, sy x sin(theta_l); above order 2 also x (NU - 1) / 2, the node scale
+  float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];
   F3 sum_r[kDensityTexelsPerTask];   // sums of L (1 + nu2^2) dw
   F3 sum_m[kDensityTexelsPerTask];   // sums of L P_M(nu2) / mie_k dw
 };
 
-// The 32 phi samples of theta row l for the texels of one task.
+// The 32 phi samples of theta row l for the texels of one task.  At order 2
+// A = mu_s cos(theta_l) and nu1 = A + sxs cos(phi) +- sys sin(phi) is formed
+// (the phase functions at nu1 need it); above order 2 A is already the node
+// coordinate of nu1 = mu_s cos(theta_l), and sxs, sys are scaled likewise, so
+// a side's coordinate is one FMA, and the ground lookup's coordinate another
+// (g_scale, g_off then map the node coordinate, not nu1).
 template <bool kOrder2, bool kGround>
 __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts& c, float A,
                                                 float B, float oxs, float dw, float half_nu,
@@ -119,17 +125,20 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
     const float pm = pr * (rs * rs * rs);
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-      const float base = fmaf(task.sxs[q], cs.x, A);   // nu1 = base +- dl
-      const float dl = task.sys[q] * cs.y;
-      const float bu = fmaf(base, half_nu, nu_off);
-      const float bg = kGround ? fmaf(base, g_scale, g_off) : 0.0f;
+      // nu1 = base +- dl (order 2); the node coordinate is bu +- sin(phi) sys.
+      const float base = kOrder2 ? fmaf(task.sxs[q], cs.x, A) : 0.0f;
+      const float dl = kOrder2 ? task.sys[q] * cs.y : 0.0f;
+      const float bu = kOrder2 ? fmaf(base, half_nu, nu_off) : fmaf(task.sxs[q], cs.x, A);
+      const float bg = kOrder2 && kGround ? fmaf(base, g_scale, g_off) : 0.0f;
       // Ls is seeded with the first side's radiance (an explicit 0 + x
       // would cost an add per channel: IEEE keeps it).
       F3 Ls;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         const float sdl = side == 0 ? dl : -dl;
-        const float u = fmaxf(fmaf(sdl, half_nu, bu), -0.5f);
+        const float ur = kOrder2 ? fmaf(sdl, half_nu, bu)
+                                 : fmaf(side == 0 ? cs.y : -cs.y, task.sys[q], bu);
+        const float u = fmaxf(ur, -0.5f);
         const float t = u + kRoundMagic;
         const F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
         if (kOrder2) {
@@ -149,7 +158,8 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
           // Ground bounce: the ground point is at radius Rb, so the cosine
           // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
           // irradiance lookup at r = Rb reads row 0 of the LUT.
-          const float x = clampf(fmaf(sdl, g_scale, bg), -0.5f, ir_top);
+          const float x =
+              clampf(kOrder2 ? fmaf(sdl, g_scale, bg) : fmaf(ur, g_scale, g_off), -0.5f, ir_top);
           Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), Ls);
         }
       }
@@ -244,19 +254,26 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     const float g_off = fmaf(fmaf(row.r * cc.mu_s, half_inv_rb, 0.5f), iw1, -0.5f);
     for (int l = 0; l < kDensityThetaSamples; ++l) {
       const DensityRow dr = drows[l];
-      const float A = cc.mu_s * dr.cos_t, B = row.mu * dr.cos_t;
+      const float B = row.mu * dr.cos_t;
       const float oxs = row.omega_x * dr.sin_t;
       const float dw = dtdp * dr.sin_t;
+      // Above order 2 in node coordinates (see DensityThetaRow).
+      const float scale = kOrder2 ? 1.0f : half_nu;
+      const float A = kOrder2 ? cc.mu_s * dr.cos_t : fmaf(cc.mu_s * dr.cos_t, half_nu, nu_off);
 #pragma unroll
       for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-        task.sxs[q] = sx[q] * dr.sin_t;
-        task.sys[q] = sy[q] * dr.sin_t;
+        task.sxs[q] = sx[q] * dr.sin_t * scale;
+        task.sys[q] = sy[q] * dr.sin_t * scale;
       }
       const uint32_t row_adj = RowAdjust(e_base + (uint32_t)(l * NU * kStride), kStride);
       if (dr.ground) {
+        // Ground texel coordinate from nu1 (order 2) or from nu1's node
+        // coordinate u = nu1 (NU - 1) / 2 + nu_off.
+        const float gs = dr.dist_ground * half_inv_rb * iw1;
+        const float gs_u = kOrder2 ? gs : gs / half_nu;
+        const float go_u = kOrder2 ? g_off : fmaf(-nu_off, gs_u, g_off);
         DensityThetaRow<kOrder2, true>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
-                                       f3(dr.t_ground), dr.dist_ground * half_inv_rb * iw1,
-                                       g_off, ir_top, ir_adj);
+                                       f3(dr.t_ground), gs_u, go_u, ir_top, ir_adj);
       } else {
         DensityThetaRow<kOrder2, false>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
                                         f3(0.0f), 0.0f, 0.0f, 0.0f, ir_adj);
