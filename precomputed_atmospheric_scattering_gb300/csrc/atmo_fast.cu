@@ -93,18 +93,18 @@ int DensityFastSmem(const Shape& s, int order) {
 constexpr int kDensityTexelsPerTask = 2;
 
 struct DensityTask {
-  // sx, sy x sin(theta_l); above order 2 also x (NU - 1) / 2, the node scale
+  // sx, sy x sin(theta_l) x (NU - 1) / 2 (in node coordinates)
   float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];
   F3 sum_r[kDensityTexelsPerTask];   // sums of L (1 + nu2^2) dw
   F3 sum_m[kDensityTexelsPerTask];   // sums of L P_M(nu2) / mie_k dw
 };
 
-// The 32 phi samples of theta row l for the texels of one task.  At order 2
-// A = mu_s cos(theta_l) and nu1 = A + sxs cos(phi) +- sys sin(phi) is formed
-// (the phase functions at nu1 need it); above order 2 A is already the node
-// coordinate of nu1 = mu_s cos(theta_l), and sxs, sys are scaled likewise, so
-// a side's coordinate is one FMA, and the ground lookup's coordinate another
-// (g_scale, g_off then map the node coordinate, not nu1).
+// The 32 phi samples of theta row l for the texels of one task.  Everything
+// is in node coordinates u = nu1 (NU - 1) / 2 + nu_off: A is the coordinate
+// of mu_s cos(theta_l), sxs and sys are scaled likewise, so a side's
+// coordinate is one FMA and the ground lookup's coordinate another (g_scale,
+// g_off map u to the irradiance texel coordinate); order 2 recovers nu1 from
+// u for its phase functions.
 template <bool kOrder2, bool kGround>
 __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts& c, float A,
                                                 float B, float oxs, float dw, float half_nu,
@@ -113,6 +113,8 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
                                                 uint32_t ir_adj) {
   constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
   const float m2g = c.m2g, g2p1 = c.g2p1;
+  // nu1 from its node coordinate u = nu1 (NU - 1) / 2 + nu_off (order 2).
+  const float inv_half_nu = 1.0f / half_nu, nu1_off = -nu_off * inv_half_nu;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
   // the outgoing direction; nu1 differs by the sign of sy sin(phi).
 #pragma unroll 2
@@ -125,19 +127,14 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
     const float pm = pr * (rs * rs * rs);
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-      // nu1 = base +- dl (order 2); the node coordinate is bu +- sin(phi) sys.
-      const float base = kOrder2 ? fmaf(task.sxs[q], cs.x, A) : 0.0f;
-      const float dl = kOrder2 ? task.sys[q] * cs.y : 0.0f;
-      const float bu = kOrder2 ? fmaf(base, half_nu, nu_off) : fmaf(task.sxs[q], cs.x, A);
-      const float bg = kOrder2 && kGround ? fmaf(base, g_scale, g_off) : 0.0f;
+      // The node coordinate of nu1: bu +- sin(phi) sys.
+      const float bu = fmaf(task.sxs[q], cs.x, A);
       // Ls is seeded with the first side's radiance (an explicit 0 + x
       // would cost an add per channel: IEEE keeps it).
       F3 Ls;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
-        const float sdl = side == 0 ? dl : -dl;
-        const float ur = kOrder2 ? fmaf(sdl, half_nu, bu)
-                                 : fmaf(side == 0 ? cs.y : -cs.y, task.sys[q], bu);
+        const float ur = fmaf(side == 0 ? cs.y : -cs.y, task.sys[q], bu);
         const float u = fmaxf(ur, -0.5f);
         const float t = u + kRoundMagic;
         const F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
@@ -146,7 +143,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
           // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
           // with the constant factors staged into the tables.
           const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
-          const float nu1 = base + sdl;
+          const float nu1 = fmaf(ur, inv_half_nu, nu1_off);
           const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
           const F3 L1 = fma3(M, r1 * r1 * r1, L);
           const float q1 = fmaf(nu1, nu1, 1.0f);
@@ -158,8 +155,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts&
           // Ground bounce: the ground point is at radius Rb, so the cosine
           // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
           // irradiance lookup at r = Rb reads row 0 of the LUT.
-          const float x =
-              clampf(kOrder2 ? fmaf(sdl, g_scale, bg) : fmaf(ur, g_scale, g_off), -0.5f, ir_top);
+          const float x = clampf(fmaf(ur, g_scale, g_off), -0.5f, ir_top);
           Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), Ls);
         }
       }
@@ -257,21 +253,18 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
       const float B = row.mu * dr.cos_t;
       const float oxs = row.omega_x * dr.sin_t;
       const float dw = dtdp * dr.sin_t;
-      // Above order 2 in node coordinates (see DensityThetaRow).
-      const float scale = kOrder2 ? 1.0f : half_nu;
-      const float A = kOrder2 ? cc.mu_s * dr.cos_t : fmaf(cc.mu_s * dr.cos_t, half_nu, nu_off);
+      // In node coordinates (see DensityThetaRow).
+      const float A = fmaf(cc.mu_s * dr.cos_t, half_nu, nu_off);
 #pragma unroll
       for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-        task.sxs[q] = sx[q] * dr.sin_t * scale;
-        task.sys[q] = sy[q] * dr.sin_t * scale;
+        task.sxs[q] = sx[q] * dr.sin_t * half_nu;
+        task.sys[q] = sy[q] * dr.sin_t * half_nu;
       }
       const uint32_t row_adj = RowAdjust(e_base + (uint32_t)(l * NU * kStride), kStride);
       if (dr.ground) {
-        // Ground texel coordinate from nu1 (order 2) or from nu1's node
-        // coordinate u = nu1 (NU - 1) / 2 + nu_off.
-        const float gs = dr.dist_ground * half_inv_rb * iw1;
-        const float gs_u = kOrder2 ? gs : gs / half_nu;
-        const float go_u = kOrder2 ? g_off : fmaf(-nu_off, gs_u, g_off);
+        // Ground texel coordinate from nu1's node coordinate.
+        const float gs_u = dr.dist_ground * half_inv_rb * iw1 / half_nu;
+        const float go_u = fmaf(-nu_off, gs_u, g_off);
         DensityThetaRow<kOrder2, true>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
                                        f3(dr.t_ground), gs_u, go_u, ir_top, ir_adj);
       } else {
