@@ -11,9 +11,11 @@ explicit L2 flush is needed between steps.
 
 Reported (one JSON line on rank 0):
   value          batched rebuilds/s (device-timed with CUDA events),
-  e2e            the same through the public C API with host buffers: the
-                 atmosphere parameters go host->device and every LUT comes
-                 back device->host into pinned memory inside the timed region,
+  e2e            the same through the public C API with host buffers: every
+                 step's atmosphere parameters go host->device and all its LUTs
+                 come back device->host into pinned memory inside the timed
+                 region (two batches alternate, so a step's read-back overlaps
+                 the next step's rebuilds),
   single_rebuild p50/p99 latency of one Model.Init (fast path) and the plain
                  path's rebuilds/s,
   roofline       the scattering-density kernel against this GPU's FP32 FMA
@@ -249,35 +251,51 @@ def run_gpu(args):
                                   device="cuda" if world > 1 else None)
 
     # --- end to end through the C API with host buffers ---------------------
+    # Every step sets its atmospheres (host -> device with the run) and reads
+    # all LUTs back into pinned host memory.  Two batches alternate so that the
+    # read-back of step k (on a copy stream) overlaps the rebuilds of step k+1.
     kinds = [atmo.LUT_TRANSMITTANCE, atmo.LUT_SCATTERING, atmo.LUT_IRRADIANCE]
     views = [batch.lut_view(0, k) for k in kinds]
     sizes = [v.width * v.height * v.depth * 16 for v in views]
-    host = [[torch.empty(s // 4, dtype=torch.float32).pin_memory() for s in sizes]
-            for _ in range(B)]
+    batches = [batch, atmo.Batch(atms, [shape] * B, 4, combined=True)]
+    host = [[[torch.empty(sz // 4, dtype=torch.float32).pin_memory() for sz in sizes]
+             for _ in range(B)] for _ in range(2)]
     import ctypes as C
-    L = atmo.lib()
     h2d = B * C.sizeof(atmo.Atmosphere)
     d2h = B * sum(sizes)
+    copy_stream = torch.cuda.Stream()
+    ran = [torch.cuda.Event(), torch.cuda.Event()]
+    copied = [None, None]
 
-    def e2e_step():
+    def e2e_step(k):
+        slot = k % 2
+        b = batches[slot]
+        if copied[slot] is not None:
+            stream.wait_event(copied[slot])      # its LUTs were read back
         for i in range(B):
-            batch.set_atmosphere(i, atms[i])
-        batch.run(stream)
+            b.set_atmosphere(i, atms[i])
+        b.run(stream)
+        ran[slot].record(stream)
+        copy_stream.wait_event(ran[slot])
         for i in range(B):
-            for k, buf, nb in zip(kinds, host[i], sizes):
-                st = L.atmo_batch_read_lut(batch._h, i, k, C.cast(buf.data_ptr(),
-                                           C.POINTER(C.c_float)), nb)
-                if st != 0:
-                    raise RuntimeError(L.atmo_last_error().decode())
-    e2e_step()
+            for kind, buf, nb in zip(kinds, host[slot][i], sizes):
+                b.copy_lut(i, kind, buf.data_ptr(), nb, copy_stream)
+        copied[slot] = torch.cuda.Event()
+        copied[slot].record(copy_stream)
+
+    e2e_step(0)
+    e2e_step(1)
+    copy_stream.synchronize()
     barrier()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(4, args.steps)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
+    for k in range(e2e_steps):
+        e2e_step(k)
+    copy_stream.synchronize()
     barrier()
     e2e_value, _ = replica_rate(time.perf_counter() - t0, B * e2e_steps, world,
                                 device="cuda" if world > 1 else None)
+    del batches[1]
 
     # --- single-instance latency (fast) and the plain path ------------------
     single = atmo.Batch([atms[0]], [shape], 4, combined=True)

@@ -261,6 +261,11 @@ atmo_status atmo_batch_get_lut(const atmo_batch* batch, unsigned i, atmo_lut_kin
                                atmo_lut_view* view);
 atmo_status atmo_batch_read_lut(const atmo_batch* batch, unsigned i, atmo_lut_kind kind,
                                 float* host_dst, size_t bytes);
+/* Copies a LUT of instance i (float32 RGBA, `bytes` = the view's bytes) to
+   `dst` (device or host memory; pinned host memory makes it asynchronous),
+   ordered on `stream` (make it wait for the run first, e.g. with an event). */
+atmo_status atmo_batch_copy_lut(const atmo_batch* batch, unsigned i, atmo_lut_kind kind,
+                                void* dst, size_t bytes, atmo_stream stream);
 /* Number of kernels one atmo_batch_run launches (for launch accounting). */
 atmo_status atmo_batch_kernel_count(const atmo_batch* batch, unsigned* count);
 /* Runs the batch once without a graph and times every kernel with CUDA

@@ -213,6 +213,7 @@ def lib():
             "atmo_batch_get_lut": [vp, C.c_uint, C.c_int, P(LutView)],
             "atmo_batch_read_lut": [vp, C.c_uint, C.c_int, P(C.c_float), C.c_size_t],
             "atmo_batch_kernel_count": [vp, P(C.c_uint)],
+            "atmo_batch_copy_lut": [vp, C.c_uint, C.c_int, vp, C.c_size_t, vp],
             "atmo_measure_fp32_peak": [P(C.c_double)],
             "atmo_batch_time_passes": [vp, vp, C.c_uint, P(C.c_float), P(C.c_int), P(C.c_int),
                                        P(C.c_uint)],
@@ -685,6 +686,11 @@ class Batch:
 
     def save_luts(self, i, directory):
         _check(lib().atmo_batch_save_luts(self._h, i, os.fsencode(directory)))
+
+    def copy_lut(self, i, kind, dst_ptr, nbytes, stream=None):
+        """Stream-ordered copy of a LUT into dst (device or pinned host)."""
+        _check(lib().atmo_batch_copy_lut(self._h, i, kind, dst_ptr, nbytes,
+                                         _stream_ptr(stream)))
 
     def lut_set(self, i) -> "LutSet":
         h = C.c_void_p()

@@ -799,6 +799,18 @@ atmo_status atmo_batch_read_lut(const atmo_batch* b, unsigned i, atmo_lut_kind k
   return ReadView(v, dst, bytes);
 }
 
+atmo_status atmo_batch_copy_lut(const atmo_batch* b, unsigned i, atmo_lut_kind kind, void* dst,
+                                size_t bytes, atmo_stream stream) {
+  if (!b || !dst || i >= b->storages.size()) return Fail(ATMO_INVALID_ARG, "bad argument");
+  atmo_lut_view v;
+  atmo_status s = ViewOf(b->storages[i], kind, &v);
+  if (s != ATMO_OK) return s;
+  if (bytes != v.bytes) return Fail(ATMO_INVALID_ARG, "destination size mismatch");
+  ATMO_CUDA_TRY(cudaMemcpyAsync(dst, v.device_ptr, bytes, cudaMemcpyDefault,
+                                reinterpret_cast<cudaStream_t>(stream)));
+  return ATMO_OK;
+}
+
 atmo_status atmo_batch_kernel_count(const atmo_batch* b, unsigned* count) {
   if (!b || !count) return Fail(ATMO_INVALID_ARG, "NULL argument");
   *count = (unsigned)b->program->KernelCount();

@@ -60,3 +60,25 @@ def test_batch_replay_and_parameter_update(atmo, oracle, torch):
     alone = gpu_precompute(atmo, torch, new, SHAPES[0], 4, True, 0)
     np.testing.assert_array_equal(b.read(1, atmo.LUT_SCATTERING), alone[1])
     assert b.kernel_count() > 0
+
+
+def test_batch_copy_lut_is_stream_ordered(atmo, oracle, torch):
+    """atmo_batch_copy_lut on a side stream, after an event of the run, gives
+    the same texels as the synchronous read, into device or pinned memory."""
+    b = atmo.Batch([oracle.earth_atmosphere()], [SHAPES[0]], 3)
+    run_stream, copy_stream = torch.cuda.Stream(), torch.cuda.Stream()
+    b.run(run_stream)
+    done = torch.cuda.Event()
+    done.record(run_stream)
+    copy_stream.wait_event(done)
+    v = b.lut_view(0, atmo.LUT_SCATTERING)
+    dev = torch.empty(v.bytes // 4, device="cuda")
+    pin = torch.empty(v.bytes // 4).pin_memory()
+    b.copy_lut(0, atmo.LUT_SCATTERING, dev.data_ptr(), v.bytes, copy_stream)
+    b.copy_lut(0, atmo.LUT_SCATTERING, pin.data_ptr(), v.bytes, copy_stream)
+    copy_stream.synchronize()
+    ref = b.read(0, atmo.LUT_SCATTERING).ravel()
+    np.testing.assert_array_equal(dev.cpu().numpy(), ref)
+    np.testing.assert_array_equal(pin.numpy(), ref)
+    with pytest.raises(atmo.AtmoError):
+        b.copy_lut(0, atmo.LUT_SCATTERING, dev.data_ptr(), v.bytes - 16, copy_stream)
