@@ -89,9 +89,12 @@ int DensityFastSmem(const Shape& s, int order) {
 }
 
 // Texels of one mu row that a thread integrates together: they share the
-// outgoing direction's phase functions.
-constexpr int kDensityTexelsPerTask = 2;
+// outgoing direction's phase functions (4 above order 2, where the registers
+// allow it; 2 at order 2, which also holds the Mie tables' lookups).
+template <bool kOrder2>
+__host__ __device__ constexpr int DensityTexelsPerTask() { return kOrder2 ? 2 : 4; }
 
+template <int kDensityTexelsPerTask>
 struct DensityTask {
   // sx, sy x sin(theta_l) x (NU - 1) / 2 (in node coordinates)
   float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];
@@ -106,12 +109,14 @@ struct DensityTask {
 // g_off map u to the irradiance texel coordinate); order 2 recovers nu1 from
 // u for its phase functions.
 template <bool kOrder2, bool kGround>
-__device__ __forceinline__ void DensityThetaRow(DensityTask& task, const Consts& c, float A,
+__device__ __forceinline__ void DensityThetaRow(DensityTask<DensityTexelsPerTask<kOrder2>()>& task,
+                                                const Consts& c, float A,
                                                 float B, float oxs, float dw, float half_nu,
                                                 float nu_off, uint32_t row_adj, F3 tg,
                                                 float g_scale, float g_off, float ir_top,
                                                 uint32_t ir_adj) {
   constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
+  constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
   // nu1 from its node coordinate u = nu1 (NU - 1) / 2 + nu_off (order 2).
   const float inv_half_nu = 1.0f / half_nu, nu1_off = -nu_off * inv_half_nu;
@@ -171,6 +176,7 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   extern __shared__ float4 smem[];
   constexpr int kSpecies = kOrder2 ? 2 : 1;
   constexpr int kStride = kSpecies * kNodeBytes;
+  constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   int local;
   const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
   const Shape s = in.s;
@@ -236,7 +242,7 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     const int j = ti % s.smu, n0 = (ti / s.smu) * kDensityTexelsPerTask;
     const TexelRow row = in.tab.rows[k * s.smu + j];
     float sx[kDensityTexelsPerTask], sy[kDensityTexelsPerTask];
-    DensityTask task;
+    DensityTask<kDensityTexelsPerTask> task;
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
       const TexelAngles ang = MakeAngles(s, row, cc, min(n0 + q, NU - 1));
