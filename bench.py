@@ -20,6 +20,8 @@ Reported (one JSON line on rank 0):
                  path's rebuilds/s,
   roofline       the scattering-density kernel against this GPU's FP32 FMA
                  throughput measured in the same run,
+  parity         per-LUT max / p99 relative error of the benchmarked LUTs at
+                 the FP64 reference's committed sampled texels,
   batched_mixed  256 seeded planets of uneven LUT shapes ({half, default,
                  double-R}) and 2-6 orders in one batched pass sequence,
   serving        a short seeded Poisson stream (2000 req/s, 10% rebuilds of
@@ -314,6 +316,9 @@ def run_gpu(args):
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
     plain_ms = time_plain(atmo, W, torch, stream, args)
 
+    # --- error of the benchmarked LUTs against the FP64 reference ------------
+    parity = parity_entry(atmo, W, batch, torch)
+
     # --- roofline of the scattering-density kernel ---------------------------
     peak = atmo.measure_fp32_peak()
     roof = roofline_entry(batch, B, peak, stream)
@@ -344,6 +349,7 @@ def run_gpu(args):
                            "plain_ms": plain_ms, "plain_rebuilds_per_s": 1000.0 / plain_ms,
                            "batched_vs_plain": value / (1000.0 / plain_ms) / world},
         "roofline": roof,
+        "parity": parity,
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clk,
     }
@@ -402,6 +408,41 @@ def roofline_entry(batch, B, peak, stream):
             "flops_per_sample": {str(k): v for k, v in DENSITY_FLOPS_PER_SAMPLE.items()},
             "passes_ms": {n + ("" if o == 0 else str(o)): round(ms, 4)
                           for n, o, ms in passes}}
+
+
+GOLDEN = os.path.join(ROOT, "tests", "golden", "earth_default.npz")
+PARITY_FLOOR = 1e-6        # relative-error floor, x the channel's largest value
+
+
+def parity_entry(atmo, W, batch, torch):
+    """Per-LUT relative error of instance 0 of the benchmarked batch against
+    the FP64 reference values committed in tests/golden/earth_default.npz
+    (the reference's own functions.glsl built as FP64 C++; sampled texels:
+    every 7th transmittance, every 61st scattering texel, all irradiance)."""
+    g = np.load(GOLDEN)
+    a = W.earth()
+    fields = [*a.solar_irradiance, a.sun_angular_radius, a.bottom_radius, a.top_radius]
+    if not np.allclose(g["atmosphere"][:6], fields, rtol=1e-12) or \
+            tuple(g["shape"]) != W.DEFAULT or int(g["orders"]) != 4:
+        return {"unavailable": "golden atmosphere differs from the benchmarked one"}
+    torch.cuda.synchronize()
+    out = {}
+    for name, kind, idx, ch in (("transmittance", atmo.LUT_TRANSMITTANCE, "transmittance_index", 3),
+                                ("scattering", atmo.LUT_SCATTERING, "scattering_index", 4),
+                                ("irradiance", atmo.LUT_IRRADIANCE, None, 3)):
+        got = batch.read(0, kind).reshape(-1, 4).astype(np.float64)
+        ref = g[name].reshape(-1, 4).astype(np.float64)
+        if idx is not None:
+            got = got[g[idx]]
+        got, ref = got[:, :ch], ref[:, :ch]
+        floor = PARITY_FLOOR * np.maximum(np.abs(ref).max(axis=0), 1e-300)
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), floor)
+        out[name] = {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                     "texels": int(ref.shape[0])}
+    out["reference"] = ("FP64 reference build (functions.glsl as C++), tests/golden/"
+                        "earth_default.npz; relative error, floor 1e-6 x channel max")
+    out["tolerance"] = {"transmittance": 1e-4, "scattering": 1e-3, "irradiance": 1e-3}
+    return out
 
 
 def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
