@@ -42,6 +42,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -172,7 +173,9 @@ class ClockSampler:
 
     def __init__(self, gpu_index):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % gpu_index)
+        # The raw samples (the JSON line carries their summary).
+        out_dir = os.environ.get("ATMO_BENCH_OUT") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, "clocks_bench_%d.csv" % gpu_index)
         self.gpu = gpu_index
 
     def __enter__(self):
