@@ -63,6 +63,11 @@ ATMO_REF_SHAPE(shape_small, 64, 16, 4, 16, 8, 4, 16, 4)
 #include "ref_passes.inc"
 ATMO_REF_SHAPE_END
 
+ATMO_REF_SHAPE(shape_small_nu128, 64, 16, 4, 16, 8, 128, 16, 4)
+#include "atmosphere/functions.glsl"
+#include "ref_passes.inc"
+ATMO_REF_SHAPE_END
+
 namespace {
 using refshim::AtmosphereParameters;
 using refshim::DensityProfile;
@@ -107,6 +112,7 @@ int ShapeId(const oracle_shape* s) {
   if (is(256, 64, 32, 128, 32, 8, 64, 16)) return 0;
   if (is(128, 32, 8, 32, 16, 8, 32, 8)) return 1;
   if (is(64, 16, 4, 16, 8, 4, 16, 4)) return 2;
+  if (is(64, 16, 4, 16, 8, 128, 16, 4)) return 3;
   return -1;
 }
 void Out3(const Spectrum& s, double* o) { o[0] = s[0]; o[1] = s[1]; o[2] = s[2]; }
@@ -117,6 +123,7 @@ void Out3(const Spectrum& s, double* o) { o[0] = s[0]; o[1] = s[1]; o[2] = s[2];
     case 0: { using namespace shape_default; __VA_ARGS__; } break; \
     case 1: { using namespace shape_medium; __VA_ARGS__; } break;  \
     case 2: { using namespace shape_small; __VA_ARGS__; } break;   \
+    case 3: { using namespace shape_small_nu128; __VA_ARGS__; } break; \
     default: return -1;                              \
   }
 

@@ -24,22 +24,32 @@ constexpr int kDensityFastThreads = 256;
 
 int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
 
-// Piecewise-linear functions staged in shared memory are stored per segment
-// [n, n + 1] as the line a + b x of the segment in the coordinate x = node
-// coordinate - 0.5 (b = the slope to the next node, 0 at the last node; a =
-// L[n] + b (0.5 - n)), so a lookup is one FMA per channel.  The segment is
-// found by rounding rather than flooring: adding 1.5 x 2^23 to x (|x| < 2^22)
-// leaves round(x) in the sum's low mantissa bits, ties to even.  With x >= -0.5
-// that selects the segment holding the coordinate (a coordinate on a node may
-// take either segment; both give the node's value).  The sum's bit pattern,
-// times the entry size, plus a row offset that cancels the constant's exponent
-// bits (mod 2^32), is the entry's shared-memory address.  The intercept's
-// cancellation costs at most ~n ulp of the node values (n < 128).
+// Piecewise-linear functions staged in shared memory.  A row of N node
+// values L[0..N-1] (node coordinate v in [0, N - 1]) is stored as N + 1
+// entries, each the line a + b s of one interval in the unit coordinate
+// s = (v + 0.5) / N: entry 0 is L[0] (v < 0), entry N is L[N - 1] (v >
+// N - 1), entry e in between the segment [e - 1, e] (b = the slope times N).
+// A lookup takes s from a saturating FMA, which clamps it to [0, 1] and maps
+// a NaN to 0, then the entry from a second FMA: s N + 1.5 x 2^23, rounded to
+// nearest, leaves round(v + 0.5), in [0, N], in the sum's low mantissa bits
+// (a v on a node may take either neighbouring entry; both give the node's
+// value).  The sum's bit pattern, times the entry size, plus a row offset
+// that cancels the constant's exponent bits (mod 2^32), is the entry's
+// shared-memory address: no index can leave the row, and the value is one
+// FMA per channel.  The intercept's cancellation costs at most ~n ulp of the
+// node values (n < 128).
 constexpr float kRoundMagic = 12582912.0f;
 constexpr uint32_t kRoundMagicBits = 0x4B400000u;
 
-// One segment entry: a.xyz, b.x | b.y, b.z, -, -.
+// One entry: a.xyz, b.x | b.y, b.z, -, -.
 constexpr int kNodeBytes = 32;
+
+// a b + c clamped to [0, 1], NaN to 0 (one FMA with the .sat modifier).
+__device__ __forceinline__ float FmaSat(float a, float b, float c) {
+  float d;
+  asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
 
 template <int kOffset>
 __device__ __forceinline__ float4 LoadShared4(uint32_t addr) {
@@ -55,38 +65,49 @@ __device__ __forceinline__ float2 LoadShared2(uint32_t addr) {
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(kOffset));
   return v;
 }
-// Segment n of a row: node values v = L[n], next = L[n + 1] (next = v at the
-// last node).
-__device__ __forceinline__ void StoreSegment(float4* entry, float4 v, float4 next, int n) {
-  const float dx = next.x - v.x, dy = next.y - v.y, dz = next.z - v.z;
-  const float c = 0.5f - float(n);
-  entry[0] = make_float4(fmaf(c, dx, v.x), fmaf(c, dy, v.y), fmaf(c, dz, v.z), dx);
-  entry[1] = make_float4(dy, dz, 0.0f, 0.0f);
+// Entry e (0 <= e <= N) of a row of N node values v[0..N-1].
+__device__ __forceinline__ void StoreEntry(float4* entry, const float4* v, int e, int N) {
+  if (e == 0 || e == N) {
+    const float4 a = v[e == 0 ? 0 : N - 1];
+    entry[0] = make_float4(a.x, a.y, a.z, 0.0f);
+    entry[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return;
+  }
+  const float4 p = v[e - 1], q = v[e];
+  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const float c = 0.5f - float(e);   // -(n + 0.5) for the segment n = e - 1
+  const float fn = float(N);
+  entry[0] = make_float4(fmaf(c, dx, p.x), fmaf(c, dy, p.y), fmaf(c, dz, p.z), dx * fn);
+  entry[1] = make_float4(dy * fn, dz * fn, 0.0f, 0.0f);
 }
-// The staged function at x = node coordinate - 0.5 (x >= -0.5), t = x + 1.5 x
-// 2^23, of the table whose entries (kStride bytes apart, the function's at
-// byte kOffset) start at row_adj + kRoundMagicBits kStride.
+// The staged function at the unit coordinate s, t = fmaf(s, N, kRoundMagic),
+// of the table whose entries (kStride bytes apart, the function's at byte
+// kOffset) start at row_adj + kRoundMagicBits kStride.
 template <int kStride, int kOffset>
-__device__ __forceinline__ F3 EvalNodes(float x, float t, uint32_t row_adj) {
+__device__ __forceinline__ F3 EvalNodes(float s, float t, uint32_t row_adj) {
   const uint32_t a = (uint32_t)__float_as_int(t) * (uint32_t)kStride + row_adj;
   const float4 p = LoadShared4<kOffset>(a);
   const float2 q = LoadShared2<kOffset + 16>(a);
-  return F3{fmaf(x, p.w, p.x), fmaf(x, q.x, p.y), fmaf(x, q.y, p.z)};
+  return F3{fmaf(s, p.w, p.x), fmaf(s, q.x, p.y), fmaf(s, q.y, p.z)};
 }
 __host__ __device__ constexpr uint32_t RowAdjust(uint32_t base, int stride) {
   return base - kRoundMagicBits * (uint32_t)stride;
 }
 
-// Shared memory of one block, bytes: [16][NU] node entries (the previous
+// Shared memory of one block, bytes: [16][NU + 1] entries (the previous
 // order interpolated in mu at the slab's r and mu_s; at order 2 a Rayleigh
-// and a Mie entry per node), the bottom row of the irradiance LUT as [IW]
+// and a Mie entry each), the bottom row of the irradiance LUT as [IW + 1]
 // entries, and a float4 staging value per node.
 int DensityFastSmem(const Shape& s, int order) {
   const int species = order == 2 ? 2 : 1;
   const int nodes = kDensityThetaSamples * s.snu;
-  return nodes * species * kNodeBytes + s.iw * kNodeBytes +
+  const int entries = kDensityThetaSamples * (s.snu + 1);
+  return entries * species * kNodeBytes + (s.iw + 1) * kNodeBytes +
          (species * nodes + s.iw) * (int)sizeof(float4);
 }
+// Shapes whose order-2 tables (the larger) fit the default 48 KB per block;
+// the others take the plain density kernel.
+bool DensityFastFits(const Shape& s) { return DensityFastSmem(s, 2) <= 48 * 1024; }
 
 // Texels of one mu row that a thread integrates together: they share the
 // outgoing direction's phase functions (4 above order 2, where the registers
@@ -94,61 +115,68 @@ int DensityFastSmem(const Shape& s, int order) {
 template <bool kOrder2>
 __host__ __device__ constexpr int DensityTexelsPerTask() { return kOrder2 ? 2 : 4; }
 
-template <int kDensityTexelsPerTask>
+// Above order 2 the outgoing direction's phase functions and the scattering
+// coefficients fold into one weight per channel and direction (shared by the
+// task's 4 texels); at order 2 (2 texels a task) the Rayleigh and Mie sums
+// stay apart, which takes fewer instructions and registers.
+template <bool kOrder2>
 struct DensityTask {
-  // sx, sy x sin(theta_l) x (NU - 1) / 2 (in node coordinates)
-  float sxs[kDensityTexelsPerTask], sys[kDensityTexelsPerTask];
-  F3 sum_r[kDensityTexelsPerTask];   // sums of L (1 + nu2^2) dw
-  F3 sum_m[kDensityTexelsPerTask];   // sums of L P_M(nu2) / mie_k dw
+  static constexpr int kN = DensityTexelsPerTask<kOrder2>();
+  float sx[kN], sy[kN];   // the sun's x, y
+  F3 sum[kN];             // order 2: sums of L P_R(nu2) dw; else L (a_R P_R + a_M P_M) dw
+  F3 sum_m[kOrder2 ? kN : 1];   // order 2: sums of L P_M(nu2) dw
 };
 
 // The 32 phi samples of theta row l for the texels of one task.  Everything
-// is in node coordinates u = nu1 (NU - 1) / 2 + nu_off: A is the coordinate
-// of mu_s cos(theta_l), sxs and sys are scaled likewise, so a side's
-// coordinate is one FMA and the ground lookup's coordinate another (g_scale,
-// g_off map u to the irradiance texel coordinate); order 2 recovers nu1 from
-// u for its phase functions.
+// is in the unit coordinate s = 1/2 + k1 nu1 (k1 = (NU - 1) / (2 NU)) of the
+// staged rows: A is s's part 1/2 + k1 mu_s cos(theta_l), hs = k1 sin(theta_l)
+// scales the direction's cos(phi), sin(phi), so a side's coordinate is one
+// FMA with the sun's sx or sy and the ground lookup's coordinate another
+// (g_scale, g_off map s to the irradiance row's unit coordinate); order 2
+// recovers nu1 = (s - 1/2) / k1 for its phase functions.  war, wam: the
+// scattering coefficients at the texel times the phase constants and dw.
 template <bool kOrder2, bool kGround>
-__device__ __forceinline__ void DensityThetaRow(DensityTask<DensityTexelsPerTask<kOrder2>()>& task,
-                                                const Consts& c, float A,
-                                                float B, float oxs, float dw, float half_nu,
-                                                float nu_off, uint32_t row_adj, F3 tg,
-                                                float g_scale, float g_off, float ir_top,
+__device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
+                                                const Consts& c, float A, float hs, float B,
+                                                float oxs, F3 war, F3 wam, float fnu,
+                                                float inv_k1, uint32_t row_adj, F3 tg,
+                                                float g_scale, float g_off, float fiw,
                                                 uint32_t ir_adj) {
   constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
-  // nu1 from its node coordinate u = nu1 (NU - 1) / 2 + nu_off (order 2).
-  const float inv_half_nu = 1.0f / half_nu, nu1_off = -nu_off * inv_half_nu;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
   // the outgoing direction; nu1 differs by the sign of sy sin(phi).
 #pragma unroll 2
   for (int m = 0; m < kDensityPhiSamples / 2; ++m) {
     const float2 cs = c_density_phi[m];
-    // Phase functions at nu2 (functions.glsl:739-747, :1245-1254), x dw.
+    // Phase functions at nu2 (functions.glsl:739-747, :1245-1254), folded
+    // with the scattering coefficients into one weight per channel.
     const float nu2 = fmaf(oxs, cs.x, B);
-    const float pr = fmaf(nu2, nu2, 1.0f) * dw;
+    const float q2 = fmaf(nu2, nu2, 1.0f);
     const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
-    const float pm = pr * (rs * rs * rs);
+    // Order 2: war.x = wam.x = dw.
+    const float pr = kOrder2 ? q2 * war.x : 0.0f, pm = kOrder2 ? pr * (rs * rs * rs) : 0.0f;
+    const F3 w = kOrder2 ? f3(0.0f) : fma3(wam, q2 * (rs * rs * rs), war * q2);
+    const float hc = cs.x * hs, hn = cs.y * hs;
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-      // The node coordinate of nu1: bu +- sin(phi) sys.
-      const float bu = fmaf(task.sxs[q], cs.x, A);
+      // The unit coordinate of nu1: bu +- sy sin(theta) sin(phi) / 2.
+      const float bu = fmaf(task.sx[q], hc, A);
       // Ls is seeded with the first side's radiance (an explicit 0 + x
       // would cost an add per channel: IEEE keeps it).
       F3 Ls;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
-        const float ur = fmaf(side == 0 ? cs.y : -cs.y, task.sys[q], bu);
-        const float u = fmaxf(ur, -0.5f);
-        const float t = u + kRoundMagic;
+        const float u = FmaSat(side == 0 ? hn : -hn, task.sy[q], bu);
+        const float t = fmaf(u, fnu, kRoundMagic);
         const F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
         if (kOrder2) {
           // Single scattering with its phase functions at nu1 (:998-1004):
           // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
           // with the constant factors staged into the tables.
           const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
-          const float nu1 = fmaf(ur, inv_half_nu, nu1_off);
+          const float nu1 = fmaf(u, inv_k1, -0.5f * inv_k1);
           const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
           const F3 L1 = fma3(M, r1 * r1 * r1, L);
           const float q1 = fmaf(nu1, nu1, 1.0f);
@@ -160,12 +188,16 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<DensityTexelsPerTask
           // Ground bounce: the ground point is at radius Rb, so the cosine
           // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
           // irradiance lookup at r = Rb reads row 0 of the LUT.
-          const float x = clampf(fmaf(ur, g_scale, g_off), -0.5f, ir_top);
-          Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, x + kRoundMagic, ir_adj), Ls);
+          const float x = FmaSat(u, g_scale, g_off);
+          Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, fmaf(x, fiw, kRoundMagic), ir_adj), Ls);
         }
       }
-      task.sum_r[q] = fma3(Ls, pr, task.sum_r[q]);
-      task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
+      if (kOrder2) {
+        task.sum[q] = fma3(Ls, pr, task.sum[q]);
+        task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
+      } else {
+        task.sum[q] = fma3(Ls, w, task.sum[q]);
+      }
     }
   }
 }
@@ -183,9 +215,10 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   const int NU = s.snu, W = s.sw();
   const int k = local / s.smus, col = local % s.smus;
   const int nodes = kDensityThetaSamples * NU;
-  float4* E = smem;                                            // [nodes][species] entries
-  float4* G = E + nodes * kSpecies * (kNodeBytes / 16);        // [iw] irradiance entries
-  float4* V = G + s.iw * (kNodeBytes / 16);                    // staging values
+  const int row_entries = NU + 1;
+  float4* E = smem;                                            // [16][NU + 1][species] entries
+  float4* G = E + kDensityThetaSamples * row_entries * kSpecies * (kNodeBytes / 16);
+  float4* V = G + (s.iw + 1) * (kNodeBytes / 16);              // [species][16][NU], [IW] values
   const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
 
   // Node values: the previous order (Rayleigh or multiple, then Mie at order
@@ -213,26 +246,26 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     V[e] = v;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < staged; e += blockDim.x) {
-    if (e < kSpecies * nodes) {
-      const int sp = e / nodes, ne = e - sp * nodes;
-      const int n = ne % NU;
-      StoreSegment(E + (ne * kSpecies + sp) * (kNodeBytes / 16), V[e],
-                   n == NU - 1 ? V[e] : V[e + 1], n);
+  const int sky_entries = kSpecies * kDensityThetaSamples * row_entries;
+  for (int e = threadIdx.x; e < sky_entries + s.iw + 1; e += blockDim.x) {
+    if (e < sky_entries) {
+      const int sp = e / (kDensityThetaSamples * row_entries);
+      const int le = e - sp * kDensityThetaSamples * row_entries;
+      const int l = le / row_entries, i = le - l * row_entries;
+      StoreEntry(E + (le * kSpecies + sp) * (kNodeBytes / 16), V + sp * nodes + l * NU, i, NU);
     } else {
-      const int i = e - kSpecies * nodes;
-      StoreSegment(G + i * (kNodeBytes / 16), V[e], i == s.iw - 1 ? V[e] : V[e + 1], i);
+      const int i = e - sky_entries;
+      StoreEntry(G + i * (kNodeBytes / 16), V + kSpecies * nodes, i, s.iw);
     }
   }
   __syncthreads();
 
   const Consts& c = in.c;
   const TexelCol cc = in.tab.cols[col];
-  const float half_nu = 0.5f * float(NU - 1);
-  const float nu_off = half_nu - 0.5f;
-  const float iw1 = float(s.iw - 1);
-  const float ir_top = float(s.iw) - 1.5f;
-  const float half_inv_rb = 0.5f / c.Rb;
+  const float fnu = float(NU), fiw = float(s.iw);
+  // s = 1/2 + k1 nu1 on the sky rows, 1/2 + kg mu_g on the irradiance row.
+  const float k1 = float(NU - 1) / (2.0f * fnu), kg = float(s.iw - 1) / (2.0f * fiw);
+  const float inv_k1 = 1.0f / k1, inv_rb = 1.0f / c.Rb;
   const float dtdp = (kPiF / 16.0f) * (kPiF / 16.0f);
   const uint32_t e_base = (uint32_t)__cvta_generic_to_shared(E);
   const uint32_t ir_adj = RowAdjust((uint32_t)__cvta_generic_to_shared(G), kNodeBytes);
@@ -241,49 +274,57 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   for (int ti = threadIdx.x; ti < tasks; ti += blockDim.x) {
     const int j = ti % s.smu, n0 = (ti / s.smu) * kDensityTexelsPerTask;
     const TexelRow row = in.tab.rows[k * s.smu + j];
-    float sx[kDensityTexelsPerTask], sy[kDensityTexelsPerTask];
-    DensityTask<kDensityTexelsPerTask> task;
+    DensityTask<kOrder2> task;
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
       const TexelAngles ang = MakeAngles(s, row, cc, min(n0 + q, NU - 1));
-      sx[q] = ang.sx;
-      sy[q] = ang.sy;
-      task.sum_r[q] = f3(0.0f);
-      task.sum_m[q] = f3(0.0f);
+      task.sx[q] = ang.sx;
+      task.sy[q] = ang.sy;
+      task.sum[q] = f3(0.0f);
+      task.sum_m[kOrder2 ? q : 0] = f3(0.0f);
     }
-    // Irradiance texel coordinate - 0.5 of the ground point at nu1 = 0:
-    // (mu_g / 2 + 1 / 2) (IW - 1) with mu_g = (r mu_s + dist nu1) / Rb.
-    const float g_off = fmaf(fmaf(row.r * cc.mu_s, half_inv_rb, 0.5f), iw1, -0.5f);
+    // The scattering coefficients at the texel, with the phase constants
+    // (order 2 applies them after the loop, which saves their registers).
+    F3 a_r = f3(0.0f), a_m = f3(0.0f);
+    if (!kOrder2) {
+      a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
+      a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+    }
+    // The ground point's mu_g = (r mu_s + dist nu1) / Rb: its irradiance
+    // coordinate 1/2 + kg mu_g is w0 + kg dist nu1 / Rb.
+    const float w0 = fmaf(row.r * cc.mu_s * inv_rb, kg, 0.5f);
     for (int l = 0; l < kDensityThetaSamples; ++l) {
       const DensityRow dr = drows[l];
       const float B = row.mu * dr.cos_t;
       const float oxs = row.omega_x * dr.sin_t;
       const float dw = dtdp * dr.sin_t;
-      // In node coordinates (see DensityThetaRow).
-      const float A = fmaf(cc.mu_s * dr.cos_t, half_nu, nu_off);
-#pragma unroll
-      for (int q = 0; q < kDensityTexelsPerTask; ++q) {
-        task.sxs[q] = sx[q] * dr.sin_t * half_nu;
-        task.sys[q] = sy[q] * dr.sin_t * half_nu;
-      }
-      const uint32_t row_adj = RowAdjust(e_base + (uint32_t)(l * NU * kStride), kStride);
+      // In the unit coordinate of nu1 (see DensityThetaRow).
+      const float A = fmaf(cc.mu_s * dr.cos_t, k1, 0.5f);
+      const float hs = k1 * dr.sin_t;
+      const uint32_t row_adj =
+          RowAdjust(e_base + (uint32_t)(l * row_entries * kStride), kStride);
       if (dr.ground) {
-        // Ground texel coordinate from nu1's node coordinate.
-        const float gs_u = dr.dist_ground * half_inv_rb * iw1 / half_nu;
-        const float go_u = fmaf(-nu_off, gs_u, g_off);
-        DensityThetaRow<kOrder2, true>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
-                                       f3(dr.t_ground), gs_u, go_u, ir_top, ir_adj);
+        // The ground point's irradiance coordinate from s = 1/2 + k1 nu1:
+        // w0 + kg dist (s - 1/2) / (k1 Rb).
+        const float gs = kg * dr.dist_ground * inv_rb * inv_k1;
+        const float go = fmaf(-0.5f, gs, w0);
+        DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, kOrder2 ? f3(dw) : a_r * dw,
+                                       kOrder2 ? f3(dw) : a_m * dw, fnu, inv_k1, row_adj,
+                                       f3(dr.t_ground), gs, go, fiw, ir_adj);
       } else {
-        DensityThetaRow<kOrder2, false>(task, c, A, B, oxs, dw, half_nu, nu_off, row_adj,
-                                        f3(0.0f), 0.0f, 0.0f, 0.0f, ir_adj);
+        DensityThetaRow<kOrder2, false>(task, c, A, hs, B, oxs, kOrder2 ? f3(dw) : a_r * dw,
+                                        kOrder2 ? f3(dw) : a_m * dw, fnu, inv_k1, row_adj,
+                                        f3(0.0f), 0.0f, 0.0f, fiw, ir_adj);
       }
     }
-    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
-    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+    if (kOrder2) {
+      a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
+      a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
+    }
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
       if (n0 + q < NU) {
-        const F3 J = a_r * task.sum_r[q] + a_m * task.sum_m[q];
+        const F3 J = kOrder2 ? a_r * task.sum[q] + a_m * task.sum_m[q] : task.sum[q];
         in.dJ[(k * s.smu + j) * W + (n0 + q) * s.smus + col] = to4(J, 1.0f);
       }
     }

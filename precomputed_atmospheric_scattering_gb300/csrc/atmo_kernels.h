@@ -24,6 +24,7 @@ cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
 // Fast path (atmo_fast.cu).
 int DensityFastTiles(const Shape& s);
 int DensityFastSmem(const Shape& s, int order);
+bool DensityFastFits(const Shape& s);
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
                               int smem_bytes, cudaStream_t st);
 // The row-restructured single-scattering kernel needs W = NU x MU_S <= 1024

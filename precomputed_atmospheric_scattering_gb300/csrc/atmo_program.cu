@@ -123,6 +123,7 @@ atmo_path PassPath(Pass pass, const Shape& s, atmo_path path) {
   if (path != ATMO_PATH_FAST) return path;
   if (pass == Pass::kMultiple && !MultipleFastFits(s)) return ATMO_PATH_PLAIN;
   if (pass == Pass::kSingle && !SingleFastFits(s)) return ATMO_PATH_PLAIN;
+  if (pass == Pass::kDensity && !DensityFastFits(s)) return ATMO_PATH_PLAIN;
   return path;
 }
 

@@ -79,6 +79,27 @@ def compare_robust(oracle, atm, shape, orders, gpu, combined, report=None):
 
 
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
+@pytest.mark.parametrize("nu", [2, 32])
+def test_extreme_nu_sizes_vs_oracle(atmo, oracle, torch, nu, path):
+    """NU = 2: the density kernel's staged rows are two nodes between their
+    end entries; NU = 32: its tables exceed 48 KB per block and the fast path
+    hands the density pass to the plain kernel.  Texels whose FP64 value
+    moves by half the tolerance when a radius moves by its FP32 rounding are
+    set aside (robust_masks, fp32=True); they are all on the zenith row (the
+    upper r-slices, where the ray to the top has length ~0)."""
+    shape = (64, 16, 4, 16, 8, nu, 16, 4)
+    atm = oracle.earth_atmosphere()
+    T, S, M, I = gpu_precompute(atmo, torch, atm, shape, 4, True, path)
+    ref, masks = robust_masks(oracle, atm, shape, 4, True, fp32=True)
+    texels = 4 * 16 * 8 * nu
+    mu_row = np.arange(texels) // (nu * 8) % 16
+    assert not (~masks["scattering"] & (mu_row != 15)).any()
+    check_masked("transmittance", T, ref.transmittance, TOL_TRANSMITTANCE, masks["transmittance"])
+    check_masked("scattering", S, ref.scattering, TOL_SCATTERING, masks["scattering"], channels=4)
+    check_masked("irradiance", I, ref.irradiance, TOL_IRRADIANCE, masks["irradiance"])
+
+
+@pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
 def test_medium_shape_random_atmospheres_vs_oracle(atmo, oracle, torch, path):
     """Non-Earth planets: seeded draws over the batched-rebuild ranges, compared
     on the texels where the FP64 reference is not rounding-dominated."""
