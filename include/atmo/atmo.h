@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ATMO_ABI_VERSION 1
+#define ATMO_ABI_VERSION 2
 
 #define ATMO_LAMBDA_R 680.0
 #define ATMO_LAMBDA_G 550.0
@@ -368,6 +368,8 @@ typedef struct {
   unsigned max_rebuilds_in_flight;   /* admitted, not yet built (0: 64; <= 4096) */
   unsigned shade_streams;            /* 0: 4 */
   int combined;                      /* combine_scattering_textures of every set */
+  unsigned admit_window_us;          /* batching window: a queued rebuild waits up to this
+                                        long for others to be admitted with it (0: none) */
 } atmo_server_config;
 typedef struct {
   int state;             /* 0 queued, 1 running, 2 done, 3 failed */

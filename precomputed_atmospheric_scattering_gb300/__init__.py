@@ -140,7 +140,8 @@ class Tuning(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_rebuilds_in_flight", C.c_uint),
-                ("shade_streams", C.c_uint), ("combined", C.c_int)]
+                ("shade_streams", C.c_uint), ("combined", C.c_int),
+                ("admit_window_us", C.c_uint)]
 
 
 class TicketInfo(C.Structure):
@@ -250,7 +251,7 @@ def lib():
             f = getattr(L, name)
             f.restype = st
             f.argtypes = args
-        if L.atmo_abi_version() != 1:
+        if L.atmo_abi_version() != 2:
             raise ImportError("libatmo_gb300.so ABI version mismatch")
         _lib = L
     return _lib
@@ -553,9 +554,9 @@ class Server:
     QUEUED, RUNNING, DONE, FAILED = range(4)
 
     def __init__(self, hbm_budget_bytes=0, max_rebuilds_in_flight=0, shade_streams=0,
-                 combined=True):
+                 combined=True, admit_window_us=0):
         cfg = ServerConfig(hbm_budget_bytes, max_rebuilds_in_flight, shade_streams,
-                           int(bool(combined)))
+                           int(bool(combined)), admit_window_us)
         h = C.c_void_p()
         _check(lib().atmo_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -304,6 +304,13 @@ bool atmo_server::EvictFor(size_t bytes) {
 // Admits pending rebuilds while rows and memory allow; returns true if any.
 bool atmo_server::Admit(std::unique_lock<std::mutex>&) {
   bool any = false;
+  // The batching window: the oldest queued rebuild waits for company until
+  // its window ends or a full batch is queued.
+  if (cfg.admit_window_us > 0 && !pending_rebuilds.empty() &&
+      pending_rebuilds.size() < free_rows.size()) {
+    const auto waited = Clock::now() - tickets[pending_rebuilds.front().ticket]->submitted;
+    if (waited < std::chrono::microseconds(cfg.admit_window_us)) return false;
+  }
   while (!pending_rebuilds.empty() && !free_rows.empty()) {
     RebuildRequest& rq = pending_rebuilds.front();
     const size_t fb = FinalBytes(rq.s, cfg.combined != 0), sb = ScratchBytes(rq.s);
@@ -511,6 +518,13 @@ bool atmo_server::LaunchShades() {
   for (auto it = pending_shades.begin(); it != pending_shades.end();) {
     auto si = slots.find(it->set_id);
     if (si == slots.end()) {
+      // A rebuild still queued for admission (batching window, budget) has
+      // no slot yet: the shading request waits for it.
+      auto ti = tickets.find(it->set_id);
+      if (ti != tickets.end() && ti->second->state.load() == Ticket::kQueued) {
+        ++it;
+        continue;
+      }
       SetError("LUT set evicted or unknown");
       FailTicket(it->ticket, ATMO_NOT_READY);
       it = pending_shades.erase(it);
@@ -618,8 +632,10 @@ atmo_status atmo_server_create(const atmo_server_config* cfg, atmo_server** out)
   if (s->cfg.hbm_budget_bytes == 0) s->cfg.hbm_budget_bytes = size_t(120) << 30;
   if (s->cfg.max_rebuilds_in_flight == 0) s->cfg.max_rebuilds_in_flight = 64;
   if (s->cfg.shade_streams == 0) s->cfg.shade_streams = 4;
-  if (s->cfg.max_rebuilds_in_flight > 4096 || s->cfg.shade_streams > 64)
-    return Fail(ATMO_INVALID_ARG, "max_rebuilds_in_flight <= 4096, shade_streams <= 64");
+  if (s->cfg.max_rebuilds_in_flight > 4096 || s->cfg.shade_streams > 64 ||
+      s->cfg.admit_window_us > 10000000)
+    return Fail(ATMO_INVALID_ARG,
+                "max_rebuilds_in_flight <= 4096, shade_streams <= 64, admit_window_us <= 1e7");
   s->stats.budget_bytes = s->cfg.hbm_budget_bytes;
   atmo_status st = s->Init();
   if (st != ATMO_OK) {

@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(atmo):
     L = C.CDLL(atmo.LIB_PATH)
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert L.atmo_abi_version() == 1
+    assert L.atmo_abi_version() == 2
 
 
 def earth_model(atmo, n_lambda=3, combined=True, half=False, shape=None):

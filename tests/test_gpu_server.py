@@ -26,6 +26,15 @@ def test_server_needs_a_device(atmo):
     assert e.value.status == atmo.CUDA_ERROR
 
 
+def test_server_config_limits(atmo):
+    """Out-of-range settings are refused before any device work."""
+    for kw in ({"max_rebuilds_in_flight": 5000}, {"shade_streams": 65},
+               {"admit_window_us": 20000000}):
+        with pytest.raises(atmo.AtmoError) as e:
+            atmo.Server(**kw)
+        assert e.value.status == atmo.INVALID_ARG
+
+
 def make_view(atmo, seed, width=96, height=54):
     rng = np.random.default_rng(seed)
     cam = rng.normal(size=3)
@@ -77,15 +86,17 @@ def test_same_alone_and_in_the_mix(atmo, oracle, torch_cuda):
     ref_sky, ref_shaded = bufs[1].cpu().numpy(), bufs[2].cpu().numpy()
     alone.close()
 
-    mix = atmo.Server(shade_streams=3)
-    tickets = []
+    # A batching window long enough that the first five rebuilds, submitted
+    # back to back, are admitted together and share their launches; the last
+    # three arrive while those run, between shading requests.
+    mix = atmo.Server(shade_streams=3, admit_window_us=100000)
+    tickets = [mix.submit_rebuild(a, s, o) for a, s, o in zip(atms[:5], shapes[:5], orders[:5])]
     keep = []
-    for i, (a, s, o) in enumerate(zip(atms, shapes, orders)):
+    for i, (a, s, o) in enumerate(zip(atms[5:], shapes[5:], orders[5:])):
+        # Shading on an earlier set while later rebuilds arrive.
+        v2, d2 = make_view(atmo, 100 + i)
+        keep.append(shade(torch, mix, tickets[i], v2, d2))
         tickets.append(mix.submit_rebuild(a, s, o))
-        if i >= 1:
-            # Shading on an earlier set while later rebuilds arrive.
-            v2, d2 = make_view(atmo, 100 + i)
-            keep.append(shade(torch, mix, tickets[i - 1], v2, d2))
     key_shade, key_bufs = shade(torch, mix, tickets[key], view, depth)
     for t in tickets:
         mix.wait(t)
