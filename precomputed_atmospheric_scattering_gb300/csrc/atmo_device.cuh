@@ -422,17 +422,25 @@ ATMO_HD float UMuFromRMu(const Consts& c, const Shape& s, const RadialPoint& p, 
 // Coordinates of one 4D lookup: the x texel column of the two nu nodes, the
 // nu lerp, and the fractional (y, z) position.
 struct Lookup4 {
-  float x0, x1;     // x coordinate in texels (before -0.5) of the two nu nodes
+  int b0, b1;       // first columns of the two nu nodes' blocks (node x MU_S)
+  float xl;         // mu_s texel coordinate within a block (after -0.5)
   float lerp_nu;
   float y, z;       // y, z texel coordinates (after -0.5)
 };
+// The reference's x texel coordinate of a nu node n is (n + u_mu_s) / NU x W
+// - 0.5 = n MU_S + (u_mu_s MU_S - 0.5).  It is kept as the block's first
+// column plus the small within-block coordinate: formed as one float, its
+// fraction would carry the rounding of n MU_S (growing with NU), and at a
+// texel-centre lookup that rounding puts a weight on the neighbouring column,
+// the previous node's brightest (highest-sun) texel.
 ATMO_HD Lookup4 MakeLookup(const Shape& s, float u_nu, float u_mu_s, float u_mu, float u_r) {
   Lookup4 L;
   float tex_coord_x = u_nu * float(s.snu - 1);
   float tex_x = floorf(tex_coord_x);
   L.lerp_nu = tex_coord_x - tex_x;
-  L.x0 = (tex_x + u_mu_s) / float(s.snu) * float(s.sw()) - 0.5f;
-  L.x1 = (tex_x + 1.0f + u_mu_s) / float(s.snu) * float(s.sw()) - 0.5f;
+  L.b0 = (int)tex_x * s.smus;
+  L.b1 = L.b0 + s.smus;
+  L.xl = fmaf(u_mu_s, float(s.smus), -0.5f);
   L.y = u_mu * float(s.smu) - 0.5f;
   L.z = u_r * float(s.sr) - 0.5f;
   return L;
@@ -441,7 +449,7 @@ ATMO_HD Lookup4 MakeLookup(const Shape& s, float u_nu, float u_mu_s, float u_mu,
 ATMO_HD int ClampIdx(int i, int n) { return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); }
 
 // The 4D lookup of functions.glsl:958-976: two trilinear fetches (the nu
-// nodes at x0 and x1) that share their y (mu) and z (r) interpolation, with
+// nodes' blocks b0 and b1) that share their y (mu) and z (r) interpolation, with
 // the nu lerp folded into the x weights.  32-bit indices (the scattering LUT
 // has fewer than 2^31 texels).
 ATMO_HD F3 Scattering4(const float4* __restrict__ tex, const Shape& s, const Lookup4& L) {
@@ -457,11 +465,11 @@ ATMO_HD F3 Scattering4(const float4* __restrict__ tex, const Shape& s, const Loo
   F3 acc = f3(0.0f);
 #pragma unroll
   for (int node = 0; node < 2; ++node) {
-    const float x = node == 0 ? L.x0 : L.x1;
+    const int base = node == 0 ? L.b0 : L.b1;
     const float wn = node == 0 ? 1.0f - L.lerp_nu : L.lerp_nu;
-    const float fx = floorf(x);
-    const float a = x - fx;
-    const int i0 = ClampIdx((int)fx, W), i1 = ClampIdx((int)fx + 1, W);
+    const float fx = floorf(L.xl);
+    const float a = L.xl - fx;
+    const int i0 = ClampIdx(base + (int)fx, W), i1 = ClampIdx(base + (int)fx + 1, W);
     const float wa0 = (1.0f - a) * wn, wa1 = a * wn;
 #ifdef __CUDA_ARCH__
 #define ATMO_TAP(idx) __ldg(tex + (idx))

@@ -43,6 +43,10 @@ constexpr uint32_t kRoundMagicBits = 0x4B400000u;
 
 // One entry: a.xyz, b.x | b.y, b.z, -, -.
 constexpr int kNodeBytes = 32;
+// One order-2 entry, the Rayleigh and the Mie lines in 48 bytes:
+// aR.xyz, bR.x | bR.yz, aM.xy | aM.z, bM.xyz.  The 48-byte stride also puts
+// the 8 entries of a 16-bank span on disjoint banks.
+constexpr int kPairBytes = 48;
 
 // a b + c clamped to [0, 1], NaN to 0 (one FMA with the .sat modifier).
 __device__ __forceinline__ float FmaSat(float a, float b, float c) {
@@ -80,6 +84,16 @@ __device__ __forceinline__ void StoreEntry(float4* entry, const float4* v, int e
   entry[0] = make_float4(fmaf(c, dx, p.x), fmaf(c, dy, p.y), fmaf(c, dz, p.z), dx * fn);
   entry[1] = make_float4(dy * fn, dz * fn, 0.0f, 0.0f);
 }
+// Entry e of a row of N Rayleigh values r[] and Mie values m[] (order 2).
+__device__ __forceinline__ void StorePairEntry(float4* entry, const float4* r, const float4* m,
+                                               int e, int N) {
+  float4 a[2], b[2];
+  StoreEntry(a, r, e, N);
+  StoreEntry(b, m, e, N);
+  entry[0] = a[0];
+  entry[1] = make_float4(a[1].x, a[1].y, b[0].x, b[0].y);
+  entry[2] = make_float4(b[0].z, b[0].w, b[1].x, b[1].y);
+}
 // The staged function at the unit coordinate s, t = fmaf(s, N, kRoundMagic),
 // of the table whose entries (kStride bytes apart, the function's at byte
 // kOffset) start at row_adj + kRoundMagicBits kStride.
@@ -89,6 +103,13 @@ __device__ __forceinline__ F3 EvalNodes(float s, float t, uint32_t row_adj) {
   const float4 p = LoadShared4<kOffset>(a);
   const float2 q = LoadShared2<kOffset + 16>(a);
   return F3{fmaf(s, p.w, p.x), fmaf(s, q.x, p.y), fmaf(s, q.y, p.z)};
+}
+// Both lines of an order-2 entry (kPairBytes apart).
+__device__ __forceinline__ void EvalPair(float s, float t, uint32_t row_adj, F3* ray, F3* mie) {
+  const uint32_t a = (uint32_t)__float_as_int(t) * (uint32_t)kPairBytes + row_adj;
+  const float4 p = LoadShared4<0>(a), q = LoadShared4<16>(a), r = LoadShared4<32>(a);
+  *ray = F3{fmaf(s, p.w, p.x), fmaf(s, q.x, p.y), fmaf(s, q.y, p.z)};
+  *mie = F3{fmaf(s, r.y, q.z), fmaf(s, r.z, q.w), fmaf(s, r.w, r.x)};
 }
 __host__ __device__ constexpr uint32_t RowAdjust(uint32_t base, int stride) {
   return base - kRoundMagicBits * (uint32_t)stride;
@@ -102,7 +123,7 @@ int DensityFastSmem(const Shape& s, int order) {
   const int species = order == 2 ? 2 : 1;
   const int nodes = kDensityThetaSamples * s.snu;
   const int entries = kDensityThetaSamples * (s.snu + 1);
-  return entries * species * kNodeBytes + (s.iw + 1) * kNodeBytes +
+  return entries * (order == 2 ? kPairBytes : kNodeBytes) + (s.iw + 1) * kNodeBytes +
          (species * nodes + s.iw) * (int)sizeof(float4);
 }
 // Shapes whose order-2 tables (the larger) fit the default 48 KB per block;
@@ -142,7 +163,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
                                                 float inv_k1, uint32_t row_adj, F3 tg,
                                                 float g_scale, float g_off, float fiw,
                                                 uint32_t ir_adj) {
-  constexpr int kStride = kOrder2 ? 2 * kNodeBytes : kNodeBytes;
+  constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
@@ -170,12 +191,16 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
       for (int side = 0; side < 2; ++side) {
         const float u = FmaSat(side == 0 ? hn : -hn, task.sy[q], bu);
         const float t = fmaf(u, fnu, kRoundMagic);
-        const F3 L = EvalNodes<kStride, 0>(u, t, row_adj);
+        F3 L, M;
+        if (kOrder2) {
+          EvalPair(u, t, row_adj, &L, &M);
+        } else {
+          L = EvalNodes<kStride, 0>(u, t, row_adj);
+        }
         if (kOrder2) {
           // Single scattering with its phase functions at nu1 (:998-1004):
           // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
           // with the constant factors staged into the tables.
-          const F3 M = EvalNodes<kStride, kNodeBytes>(u, t, row_adj);
           const float nu1 = fmaf(u, inv_k1, -0.5f * inv_k1);
           const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
           const F3 L1 = fma3(M, r1 * r1 * r1, L);
@@ -207,7 +232,7 @@ __global__ void __launch_bounds__(kDensityFastThreads)
 k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   extern __shared__ float4 smem[];
   constexpr int kSpecies = kOrder2 ? 2 : 1;
-  constexpr int kStride = kSpecies * kNodeBytes;
+  constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   int local;
   const Instance& in = insts[FindEntry(wl, blockIdx.x, &local)];
@@ -216,8 +241,8 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   const int k = local / s.smus, col = local % s.smus;
   const int nodes = kDensityThetaSamples * NU;
   const int row_entries = NU + 1;
-  float4* E = smem;                                            // [16][NU + 1][species] entries
-  float4* G = E + kDensityThetaSamples * row_entries * kSpecies * (kNodeBytes / 16);
+  float4* E = smem;                                            // [16][NU + 1] entries
+  float4* G = E + kDensityThetaSamples * row_entries * (kStride / 16);
   float4* V = G + (s.iw + 1) * (kNodeBytes / 16);              // [species][16][NU], [IW] values
   const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
 
@@ -246,13 +271,15 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     V[e] = v;
   }
   __syncthreads();
-  const int sky_entries = kSpecies * kDensityThetaSamples * row_entries;
+  const int sky_entries = kDensityThetaSamples * row_entries;
   for (int e = threadIdx.x; e < sky_entries + s.iw + 1; e += blockDim.x) {
     if (e < sky_entries) {
-      const int sp = e / (kDensityThetaSamples * row_entries);
-      const int le = e - sp * kDensityThetaSamples * row_entries;
-      const int l = le / row_entries, i = le - l * row_entries;
-      StoreEntry(E + (le * kSpecies + sp) * (kNodeBytes / 16), V + sp * nodes + l * NU, i, NU);
+      const int l = e / row_entries, i = e - l * row_entries;
+      if (kOrder2) {
+        StorePairEntry(E + e * (kPairBytes / 16), V + l * NU, V + nodes + l * NU, i, NU);
+      } else {
+        StoreEntry(E + e * (kNodeBytes / 16), V + l * NU, i, NU);
+      }
     } else {
       const int i = e - sky_entries;
       StoreEntry(G + i * (kNodeBytes / 16), V + kSpecies * nodes, i, s.iw);
@@ -478,7 +505,8 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
   const int nmax = W - 1;
   const float inv_range = 1.0f / (c.H - (c.Rt - c.Rb));
   const float inv_A = 1.0f / c.mus_A;
-  float rmu_s[kCols], nu[kCols], xb[kCols], lnu[kCols];
+  float rmu_s[kCols], nu[kCols], lnu[kCols];
+  int xb[kCols];
   F3 acc[kCols];
   if (active) {
     const TexelRow row = in.tab.rows[rowi];
@@ -495,7 +523,7 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
       const float tex_coord_x = (ang.nu + 1.0f) * 0.5f * float(s.snu - 1);
       const float tex_x = ang.on_node ? float(n) : floorf(tex_coord_x);
       lnu[m] = ang.on_node ? 0.0f : tex_coord_x - tex_x;
-      xb[m] = tex_x * smus_f - 0.5f;
+      xb[m] = (int)tex_x * s.smus;   // the node's block (see MakeLookup)
       acc[m] = f3(0.0f);
     }
   }
@@ -534,10 +562,10 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
           if (kCols > 1 && x_t + m * kMultipleFastThreads >= W) break;
           const float mu_s_i = clampf(fmaf(sm.d, nu[m], rmu_s[m]) * sm.inv_r, -1.0f, 1.0f);
           const float x0 =
-              fmaf(UMuSFromMuSAlongRay(c, s, mu_s_i, inv_range, inv_A), smus_f, xb[m]);
+              fmaf(UMuSFromMuSAlongRay(c, s, mu_s_i, inv_range, inv_A), smus_f, -0.5f);
           const float fx = floorf(x0);
           const float a = x0 - fx;
-          const int i0 = (int)fx;
+          const int i0 = xb[m] + (int)fx;
           const int c0 = min(max(i0, 0), nmax), c1 = min(max(i0 + 1, 0), nmax);
           const int c2 = min(max(i0 + s.smus, 0), nmax), c3 = min(max(i0 + s.smus + 1, 0), nmax);
           const float l1 = lnu[m], l0 = 1.0f - l1;

@@ -46,11 +46,11 @@ __device__ float4 ScatteringRGBA(const float4* __restrict__ tex, const Shape& s,
   float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
   for (int node = 0; node < 2; ++node) {
-    const float x = node == 0 ? L.x0 : L.x1;
+    const int base = node == 0 ? L.b0 : L.b1;
     const float wn = node == 0 ? 1.0f - L.lerp_nu : L.lerp_nu;
-    const float fx = floorf(x);
-    const float a = x - fx;
-    const int i0 = ClampIdx((int)fx, W), i1 = ClampIdx((int)fx + 1, W);
+    const float fx = floorf(L.xl);
+    const float a = L.xl - fx;
+    const int i0 = ClampIdx(base + (int)fx, W), i1 = ClampIdx(base + (int)fx + 1, W);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float4 t0 = __ldg(tex + rows[q] + i0), t1 = __ldg(tex + rows[q] + i1);

@@ -58,18 +58,15 @@ PERTURBATION = 1e-13
 ROBUST_THRESHOLD = 1e-5
 
 
-# FP32 conditioning (extreme LUT shapes).  The GPU holds the radii in FP32,
-# whose rounding moves each by up to ~6e-8 relative; derived quantities move
-# likewise.  Where the exact value itself moves by more than half the
-# tolerance when the top or the bottom radius alone moves by FP32_PERTURBATION,
-# an FP32 evaluation cannot be held to the tolerance (seen at NU = 128 on the
-# zenith rows at the lowest sun, deep in the planet's shadow, where a 1e-7
-# shift of the top radius moves the FP64 value by ~9%).
-FP32_PERTURBATION = 6e-8
-
-
-def _moved(base, pert, combined, threshold):
-    out = {}
+def robust_masks(O, atm, shape, orders, combined=True, base=None):
+    """Masks of the texels to compare: True where the oracle's value is not
+    dominated by FP64 rounding."""
+    b = O.Atmosphere.from_buffer_copy(bytes(atm))
+    b.bottom_radius *= 1.0 + PERTURBATION
+    b.top_radius *= 1.0 + PERTURBATION
+    base = base or O.precompute(atm, shape, orders, combined=combined)
+    pert = O.precompute(b, shape, orders, combined=combined)
+    masks = {}
     for k in ("transmittance", "scattering", "single_mie", "irradiance"):
         ch = 4 if (k == "scattering" and combined) else 3
         x = np.asarray(getattr(base, k))[..., :ch].reshape(-1, ch)
@@ -77,31 +74,7 @@ def _moved(base, pert, combined, threshold):
         scale = np.abs(x).max(axis=0)
         scale = np.where(scale > 0, scale, 1.0)
         den = np.maximum(np.abs(x), FLOOR * scale)
-        out[k] = (np.abs(x - y) / den).max(axis=1) > threshold
-    return out
-
-
-def robust_masks(O, atm, shape, orders, combined=True, base=None, fp32=False):
-    """Masks of the texels to compare: True where the oracle's value is
-    well conditioned (FP64 rounding; with fp32, also FP32 rounding of the
-    radii, threshold half the scattering tolerance)."""
-    base = base or O.precompute(atm, shape, orders, combined=combined)
-    perturbed = []
-    b = O.Atmosphere.from_buffer_copy(bytes(atm))
-    b.bottom_radius *= 1.0 + PERTURBATION
-    b.top_radius *= 1.0 + PERTURBATION
-    perturbed.append((b, ROBUST_THRESHOLD))
-    if fp32:
-        for field in ("top_radius", "bottom_radius"):
-            b = O.Atmosphere.from_buffer_copy(bytes(atm))
-            setattr(b, field, getattr(b, field) * (1.0 + FP32_PERTURBATION))
-            perturbed.append((b, 0.5 * TOL_SCATTERING))
-    masks = None
-    for b, threshold in perturbed:
-        moved = _moved(base, O.precompute(b, shape, orders, combined=combined), combined,
-                       threshold)
-        masks = {k: ~v for k, v in moved.items()} if masks is None else \
-            {k: masks[k] & ~moved[k] for k in masks}
+        masks[k] = (np.abs(x - y) / den).max(axis=1) <= ROBUST_THRESHOLD
     return base, masks
 
 

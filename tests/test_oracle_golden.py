@@ -76,8 +76,9 @@ def test_oracle_against_reference_build(oracle):
     (skipped where the reference sources are not present)."""
     if oracle.ref_lib() is None:
         pytest.skip("reference build oracle/_ref not present on this machine")
-    for shp in (oracle.SMALL_SHAPE, oracle.MEDIUM_SHAPE):
-        for combined in (True, False):
+    wide_nu = (64, 16, 4, 16, 8, 128, 16, 4)   # 128 nu nodes: lookups far from column 0
+    for shp in (oracle.SMALL_SHAPE, oracle.MEDIUM_SHAPE, wide_nu):
+        for combined in ((True,) if shp == wide_nu else (True, False)):
             atm = oracle.earth_atmosphere(mie_g=0.7, ground_albedo=0.3)
             a = oracle.precompute(atm, shp, 3, combined=combined)
             b = oracle.precompute(atm, shp, 3, combined=combined, use_reference=True)
