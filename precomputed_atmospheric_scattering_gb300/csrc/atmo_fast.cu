@@ -69,20 +69,29 @@ __device__ __forceinline__ float2 LoadShared2(uint32_t addr) {
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(kOffset));
   return v;
 }
-// Entry e (0 <= e <= N) of a row of N node values v[0..N-1].
-__device__ __forceinline__ void StoreEntry(float4* entry, const float4* v, int e, int N) {
+// The line a + b s of entry e (0 <= e <= N) of a row of N node values v[].
+__device__ __forceinline__ void EntryLine(const float4* v, int e, int N, F3* a, F3* b) {
   if (e == 0 || e == N) {
-    const float4 a = v[e == 0 ? 0 : N - 1];
-    entry[0] = make_float4(a.x, a.y, a.z, 0.0f);
-    entry[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 p = v[e == 0 ? 0 : N - 1];
+    *a = F3{p.x, p.y, p.z};
+    *b = f3(0.0f);
     return;
   }
   const float4 p = v[e - 1], q = v[e];
-  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const F3 d{q.x - p.x, q.y - p.y, q.z - p.z};
   const float c = 0.5f - float(e);   // -(n + 0.5) for the segment n = e - 1
-  const float fn = float(N);
-  entry[0] = make_float4(fmaf(c, dx, p.x), fmaf(c, dy, p.y), fmaf(c, dz, p.z), dx * fn);
-  entry[1] = make_float4(dy * fn, dz * fn, 0.0f, 0.0f);
+  *a = fma3(d, c, F3{p.x, p.y, p.z});
+  *b = d * float(N);
+}
+__device__ __forceinline__ void StoreLine(float4* entry, F3 a, F3 b) {
+  entry[0] = make_float4(a.x, a.y, a.z, b.x);
+  entry[1] = make_float4(b.y, b.z, 0.0f, 0.0f);
+}
+// Entry e (0 <= e <= N) of a row of N node values v[0..N-1].
+__device__ __forceinline__ void StoreEntry(float4* entry, const float4* v, int e, int N) {
+  F3 a, b;
+  EntryLine(v, e, N, &a, &b);
+  StoreLine(entry, a, b);
 }
 // Entry e of a row of N Rayleigh values r[] and Mie values m[] (order 2).
 __device__ __forceinline__ void StorePairEntry(float4* entry, const float4* r, const float4* m,
@@ -115,20 +124,49 @@ __host__ __device__ constexpr uint32_t RowAdjust(uint32_t base, int stride) {
   return base - kRoundMagicBits * (uint32_t)stride;
 }
 
-// Shared memory of one block, bytes: [16][NU + 1] entries (the previous
-// order interpolated in mu at the slab's r and mu_s; at order 2 a Rayleigh
-// and a Mie entry each), the bottom row of the irradiance LUT as [IW + 1]
-// entries, and a float4 staging value per node.
-int DensityFastSmem(const Shape& s, int order) {
+// Ground rows above order 2.  On a theta row whose directions hit the ground
+// the incoming radiance is the sky line (entry i, in s) plus tg times the
+// irradiance line (entry j, in the ground coordinate x = gs s + go), and on
+// each (i, j) pair their sum is one line in s.  A merged table of (NU + 1) x J
+// entries per row (J = the ground entries the row can reach) turns the ground
+// lookup into a second index: x and its entry come from the same saturating
+// and rounding FMAs as the separate lookup, monotone in s, so the entries
+// reached lie between those of s = 0 and s = 1 and no index leaves the table.
+// Rows are merged in theta order while their tables fit the budget; the
+// others keep the separate lookups.
+struct MergeRow {
+  float gs, go;       // x = gs s + go (the same values build and read the table)
+  uint32_t adj;       // address adjustment of the row's table
+  uint32_t jstride;   // J x kNodeBytes; 0 when the row is not merged
+};
+constexpr int kMergeBudgetCap = 24 * 1024;
+
+// Shared memory of one block, bytes, without the merged tables: [16][NU + 1]
+// entries (the previous order interpolated in mu at the slab's r and mu_s;
+// at order 2 a Rayleigh and a Mie line each), the bottom row of the
+// irradiance LUT as [IW + 1] entries, a float4 staging value per node, and
+// above order 2 the merge rows' descriptors and the merged entry count.
+__host__ __device__ inline int DensityBaseSmem(const Shape& s, int order) {
   const int species = order == 2 ? 2 : 1;
   const int nodes = kDensityThetaSamples * s.snu;
   const int entries = kDensityThetaSamples * (s.snu + 1);
   return entries * (order == 2 ? kPairBytes : kNodeBytes) + (s.iw + 1) * kNodeBytes +
-         (species * nodes + s.iw) * (int)sizeof(float4);
+         (species * nodes + s.iw) * 16 +
+         (order == 2 ? 0 : kDensityThetaSamples * (int)(sizeof(MergeRow) + sizeof(int4)) + 16);
+}
+// The merged tables' budget above order 2: what keeps the block within 48 KB,
+// at most kMergeBudgetCap.
+__host__ __device__ inline int DensityMergeBytes(const Shape& s) {
+  int b = 48 * 1024 - DensityBaseSmem(s, 3);
+  b = b < 0 ? 0 : (b > kMergeBudgetCap ? kMergeBudgetCap : b);
+  return b / kNodeBytes * kNodeBytes;
+}
+int DensityFastSmem(const Shape& s, int order) {
+  return DensityBaseSmem(s, order) + (order == 2 ? 0 : DensityMergeBytes(s));
 }
 // Shapes whose order-2 tables (the larger) fit the default 48 KB per block;
 // the others take the plain density kernel.
-bool DensityFastFits(const Shape& s) { return DensityFastSmem(s, 2) <= 48 * 1024; }
+bool DensityFastFits(const Shape& s) { return DensityBaseSmem(s, 2) <= 48 * 1024; }
 
 // Texels of one mu row that a thread integrates together: they share the
 // outgoing direction's phase functions (4 above order 2, where the registers
@@ -156,13 +194,17 @@ struct DensityTask {
 // (g_scale, g_off map s to the irradiance row's unit coordinate); order 2
 // recovers nu1 = (s - 1/2) / k1 for its phase functions.  war, wam: the
 // scattering coefficients at the texel times the phase constants and dw.
-template <bool kOrder2, bool kGround>
+// kMerged (ground rows above order 2): the row's merged table (MergeRow)
+// replaces the sky and ground lookups.
+template <bool kOrder2, bool kGround, bool kMerged = false>
 __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
                                                 const Consts& c, float A, float hs, float B,
                                                 float oxs, F3 war, F3 wam, float fnu,
                                                 float inv_k1, uint32_t row_adj, F3 tg,
                                                 float g_scale, float g_off, float fiw,
-                                                uint32_t ir_adj) {
+                                                uint32_t ir_adj, uint32_t jstride = 0,
+                                                uint32_t madj = 0) {
+  static_assert(!kMerged || (kGround && !kOrder2), "merged tables: ground rows above order 2");
   constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
@@ -191,6 +233,19 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
       for (int side = 0; side < 2; ++side) {
         const float u = FmaSat(side == 0 ? hn : -hn, task.sy[q], bu);
         const float t = fmaf(u, fnu, kRoundMagic);
+        if (kMerged) {
+          // Entry (i, j) of the merged table: one line in s for sky + ground.
+          const float x = FmaSat(u, g_scale, g_off);
+          const uint32_t a = (uint32_t)__float_as_int(t) * jstride +
+                             (uint32_t)__float_as_int(fmaf(x, fiw, kRoundMagic)) *
+                                 (uint32_t)kNodeBytes +
+                             madj;
+          const float4 p = LoadShared4<0>(a);
+          const float2 r = LoadShared2<16>(a);
+          const F3 L{fmaf(u, p.w, p.x), fmaf(u, r.x, p.y), fmaf(u, r.y, p.z)};
+          Ls = side == 0 ? L : Ls + L;
+          continue;
+        }
         F3 L, M;
         if (kOrder2) {
           EvalPair(u, t, row_adj, &L, &M);
@@ -244,7 +299,19 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   float4* E = smem;                                            // [16][NU + 1] entries
   float4* G = E + kDensityThetaSamples * row_entries * (kStride / 16);
   float4* V = G + (s.iw + 1) * (kNodeBytes / 16);              // [species][16][NU], [IW] values
+  // Above order 2: the merge rows, their table layout (offset, J, j0, size in
+  // entries; size 0 when not merged) and the merged tables.
+  MergeRow* meta = reinterpret_cast<MergeRow*>(V + kSpecies * nodes + s.iw);
+  int4* build = reinterpret_cast<int4*>(meta + kDensityThetaSamples);
+  int& merged_entries = *reinterpret_cast<int*>(build + kDensityThetaSamples);
+  float4* X = reinterpret_cast<float4*>(build + kDensityThetaSamples + 1);
   const DensityRow* drows = in.tab.drows + k * kDensityThetaSamples;
+  const Consts& c = in.c;
+  const TexelCol cc = in.tab.cols[col];
+  const float fnu = float(NU), fiw = float(s.iw);
+  // s = 1/2 + k1 nu1 on the sky rows, 1/2 + kg mu_g on the irradiance row.
+  const float k1 = float(NU - 1) / (2.0f * fnu), kg = float(s.iw - 1) / (2.0f * fiw);
+  const float inv_k1 = 1.0f / k1, inv_rb = 1.0f / c.Rb;
 
   // Node values: the previous order (Rayleigh or multiple, then Mie at order
   // 2) at column n MU_S + col of slice k, bilinear in mu; then the irradiance.
@@ -270,9 +337,56 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
     }
     V[e] = v;
   }
+  if (!kOrder2 && threadIdx.x < kDensityThetaSamples) {
+    // Row l's ground coordinate and the ground entries j0..j1 it can reach.
+    const int l = threadIdx.x;
+    const DensityRow dr = drows[l];
+    MergeRow mr{0.0f, 0.0f, 0u, 0u};
+    int4 b = make_int4(0, 0, 0, 0);
+    if (dr.ground) {
+      // The ground point's mu_g = (r mu_s + dist nu1) / Rb: its irradiance
+      // coordinate 1/2 + kg mu_g is w0 + kg dist (s - 1/2) / (k1 Rb).
+      const float w0 = fmaf(in.tab.rows[k * s.smu].r * cc.mu_s * inv_rb, kg, 0.5f);
+      mr.gs = kg * dr.dist_ground * inv_rb * inv_k1;
+      mr.go = fmaf(-0.5f, mr.gs, w0);
+      const int j0 = __float_as_int(fmaf(FmaSat(0.0f, mr.gs, mr.go), fiw, kRoundMagic)) -
+                     (int)kRoundMagicBits;
+      const int j1 = __float_as_int(fmaf(FmaSat(1.0f, mr.gs, mr.go), fiw, kRoundMagic)) -
+                     (int)kRoundMagicBits;
+      if (j1 >= j0) b = make_int4(0, j1 - j0 + 1, j0, (NU + 1) * (j1 - j0 + 1));
+    }
+    meta[l] = mr;
+    build[l] = b;
+  }
+  __syncthreads();
+  if (!kOrder2 && threadIdx.x == 0) {
+    // Table offsets, rows in theta order while they fit the budget.
+    const int budget = DensityMergeBytes(s) / kNodeBytes;
+    const uint32_t xbase = (uint32_t)__cvta_generic_to_shared(X);
+    int off = 0;
+    for (int l = 0; l < kDensityThetaSamples; ++l) {
+      int4 b = build[l];
+      if (b.w > 0 && off + b.w <= budget) {
+        b.x = off;
+        const uint32_t js = (uint32_t)(b.y * kNodeBytes);
+        meta[l].jstride = js;
+        // Entry (i, j) at X + off + i J + (j - j0), addressed from the two
+        // rounding sums (magic + i, magic + j).
+        meta[l].adj = xbase + (uint32_t)(off * kNodeBytes) - kRoundMagicBits * js -
+                      (kRoundMagicBits + (uint32_t)b.z) * (uint32_t)kNodeBytes;
+        off += b.w;
+      } else {
+        b.w = 0;
+      }
+      build[l] = b;
+    }
+    merged_entries = off;
+  }
   __syncthreads();
   const int sky_entries = kDensityThetaSamples * row_entries;
-  for (int e = threadIdx.x; e < sky_entries + s.iw + 1; e += blockDim.x) {
+  const int base_entries = sky_entries + s.iw + 1;
+  const int total_entries = base_entries + (kOrder2 ? 0 : merged_entries);
+  for (int e = threadIdx.x; e < total_entries; e += blockDim.x) {
     if (e < sky_entries) {
       const int l = e / row_entries, i = e - l * row_entries;
       if (kOrder2) {
@@ -280,19 +394,27 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
       } else {
         StoreEntry(E + e * (kNodeBytes / 16), V + l * NU, i, NU);
       }
-    } else {
+    } else if (e < base_entries) {
       const int i = e - sky_entries;
       StoreEntry(G + i * (kNodeBytes / 16), V + kSpecies * nodes, i, s.iw);
+    } else if (!kOrder2) {
+      // Merged entry (i, j) of row l: sky line + tg (ground line at gs s + go).
+      const int m = e - base_entries;
+      int l = 0;
+      while (l < kDensityThetaSamples - 1 && !(build[l].w > 0 && m < build[l].x + build[l].w)) ++l;
+      const int4 b = build[l];
+      const int idx = m - b.x, i = idx / b.y, j = b.z + (idx - i * b.y);
+      F3 sa, sb, ga, gb;
+      EntryLine(V + l * NU, i, NU, &sa, &sb);
+      EntryLine(V + nodes, j, s.iw, &ga, &gb);
+      const F3 tg = f3(drows[l].t_ground);
+      const MergeRow mr = meta[l];
+      StoreLine(X + m * (kNodeBytes / 16), fma3(tg, fma3(gb, mr.go, ga), sa),
+                fma3(tg, gb * mr.gs, sb));
     }
   }
   __syncthreads();
 
-  const Consts& c = in.c;
-  const TexelCol cc = in.tab.cols[col];
-  const float fnu = float(NU), fiw = float(s.iw);
-  // s = 1/2 + k1 nu1 on the sky rows, 1/2 + kg mu_g on the irradiance row.
-  const float k1 = float(NU - 1) / (2.0f * fnu), kg = float(s.iw - 1) / (2.0f * fiw);
-  const float inv_k1 = 1.0f / k1, inv_rb = 1.0f / c.Rb;
   const float dtdp = (kPiF / 16.0f) * (kPiF / 16.0f);
   const uint32_t e_base = (uint32_t)__cvta_generic_to_shared(E);
   const uint32_t ir_adj = RowAdjust((uint32_t)__cvta_generic_to_shared(G), kNodeBytes);
@@ -317,8 +439,8 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
       a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
       a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
     }
-    // The ground point's mu_g = (r mu_s + dist nu1) / Rb: its irradiance
-    // coordinate 1/2 + kg mu_g is w0 + kg dist nu1 / Rb.
+    // Order 2: the ground point's mu_g = (r mu_s + dist nu1) / Rb; its
+    // irradiance coordinate 1/2 + kg mu_g is w0 + kg dist nu1 / Rb.
     const float w0 = fmaf(row.r * cc.mu_s * inv_rb, kg, 0.5f);
     for (int l = 0; l < kDensityThetaSamples; ++l) {
       const DensityRow dr = drows[l];
@@ -331,13 +453,25 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
       const uint32_t row_adj =
           RowAdjust(e_base + (uint32_t)(l * row_entries * kStride), kStride);
       if (dr.ground) {
-        // The ground point's irradiance coordinate from s = 1/2 + k1 nu1:
-        // w0 + kg dist (s - 1/2) / (k1 Rb).
-        const float gs = kg * dr.dist_ground * inv_rb * inv_k1;
-        const float go = fmaf(-0.5f, gs, w0);
-        DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, kOrder2 ? f3(dw) : a_r * dw,
-                                       kOrder2 ? f3(dw) : a_m * dw, fnu, inv_k1, row_adj,
-                                       f3(dr.t_ground), gs, go, fiw, ir_adj);
+        if constexpr (kOrder2) {
+          // The ground point's irradiance coordinate from s = 1/2 + k1 nu1:
+          // w0 + kg dist (s - 1/2) / (k1 Rb).
+          const float gs = kg * dr.dist_ground * inv_rb * inv_k1;
+          const float go = fmaf(-0.5f, gs, w0);
+          DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, f3(dw), f3(dw), fnu, inv_k1,
+                                         row_adj, f3(dr.t_ground), gs, go, fiw, ir_adj);
+        } else {
+          const MergeRow mr = meta[l];
+          if (mr.jstride != 0) {
+            DensityThetaRow<kOrder2, true, true>(task, c, A, hs, B, oxs, a_r * dw, a_m * dw,
+                                                 fnu, inv_k1, row_adj, f3(0.0f), mr.gs, mr.go,
+                                                 fiw, ir_adj, mr.jstride, mr.adj);
+          } else {
+            DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, a_r * dw, a_m * dw, fnu,
+                                           inv_k1, row_adj, f3(dr.t_ground), mr.gs, mr.go, fiw,
+                                           ir_adj);
+          }
+        }
       } else {
         DensityThetaRow<kOrder2, false>(task, c, A, hs, B, oxs, kOrder2 ? f3(dw) : a_r * dw,
                                         kOrder2 ? f3(dw) : a_m * dw, fnu, inv_k1, row_adj,
