@@ -169,15 +169,16 @@ int DensityFastSmem(const Shape& s, int order) {
 bool DensityFastFits(const Shape& s) { return DensityBaseSmem(s, 2) <= 48 * 1024; }
 
 // Texels of one mu row that a thread integrates together: they share the
-// outgoing direction's phase functions (4 above order 2, where the registers
-// allow it; 2 at order 2, which also holds the Mie tables' lookups).
+// outgoing direction's phase functions (4 at every order: at order 2, 128
+// registers and 2 blocks per SM beat 2 texels at 80 registers and 3 blocks
+// by ~3%).
 template <bool kOrder2>
-__host__ __device__ constexpr int DensityTexelsPerTask() { return kOrder2 ? 2 : 4; }
+__host__ __device__ constexpr int DensityTexelsPerTask() { return 4; }
 
 // Above order 2 the outgoing direction's phase functions and the scattering
 // coefficients fold into one weight per channel and direction (shared by the
-// task's 4 texels); at order 2 (2 texels a task) the Rayleigh and Mie sums
-// stay apart, which takes fewer instructions and registers.
+// task's 4 texels); at order 2 the Rayleigh and Mie sums stay apart (the
+// ground term joins after the single-scattering phase functions).
 template <bool kOrder2>
 struct DensityTask {
   static constexpr int kN = DensityTexelsPerTask<kOrder2>();
