@@ -57,11 +57,12 @@ WORKLOAD = ("Earth atmosphere LUT rebuild, 256x64 / 256x128x32 / 64x16 RGBA FP32
 # FP32 operations per direction sample of the fast scattering-density kernel
 # (FADD + FMUL + 2 x FFMA, counted by ncu's SASS op counters over one launch:
 # profiles/fast_kernels_earth_default_batch2.md): order 2 evaluates single
-# scattering with its phase functions, higher orders one radiance table.
-DENSITY_FLOPS_PER_SAMPLE = {2: 50.6, 3: 26.3}
+# scattering with its phase functions, higher orders one radiance table (one
+# merged sky + ground table on the rows that hit the ground).
+DENSITY_FLOPS_PER_SAMPLE = {2: 50.9, 3: 20.1}
 # DRAM bytes per density launch and instance, from the same capture
 # (dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance launch / 2).
-DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.22e6}
+DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.24e6}
 
 
 def parse():
