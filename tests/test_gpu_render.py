@@ -138,7 +138,7 @@ class OracleRender:
         return a, b
 
 
-def oracle_outputs(ref, q, rng, perturb):
+def oracle_outputs(ref, q, rng, perturb, position=ROBUST_POSITION):
     cam, view, sun, point, normal, shadow = q
     n = len(cam)
     outs = {k: np.zeros((n, 3)) for k in ("sky", "sky_t", "pt", "pt_t", "sun", "skyirr")}
@@ -147,7 +147,7 @@ def oracle_outputs(ref, q, rng, perturb):
         return u / np.linalg.norm(u)
 
     def move(x):
-        return x + rng.normal(size=3) * ROBUST_POSITION * np.linalg.norm(x)
+        return x + rng.normal(size=3) * position * np.linalg.norm(x)
 
     for i in range(n):
         c, v, p, s, nm = cam[i], view[i], point[i], sun[i], normal[i]
@@ -172,7 +172,7 @@ def gpu_outputs(torch, lut_set, q):
              ("skyirr", sk))}
 
 
-def compare(ref_out, pert_out, gpu_out, what, terms=None, factor=None):
+def compare(ref_out, pert_out, gpu_out, what, terms=None, factor=None, min_robust=0.85):
     bad = []
     for k in ref_out:
         o, g, p = ref_out[k], gpu_out[k], pert_out[k]
@@ -186,7 +186,7 @@ def compare(ref_out, pert_out, gpu_out, what, terms=None, factor=None):
                         axis=1)
         rel = np.abs(g - o) / np.maximum(np.abs(o), floor)
         worst = rel[robust].max() if robust.any() else 0.0
-        assert robust.mean() > 0.85, (what, k, robust.mean())
+        assert robust.mean() > min_robust, (what, k, robust.mean())
         assert np.all(np.isfinite(g)), (what, k)
         i = int(np.argmax(np.where(robust[:, None], rel, 0.0)) // 3)
         print("%s %-7s worst %.3g at %d (%d robust of %d)" % (what, k, worst, i,
@@ -338,3 +338,70 @@ def test_shade_view_equals_queries(atmo, torch):
     torch.testing.assert_close(sky.reshape(-1, 4)[:, :3], r_sky, rtol=2e-4, atol=1e-7)
     torch.testing.assert_close(sky.reshape(-1, 4)[:, 3], t_sky[:, 1], rtol=2e-4, atol=1e-7)
     torch.testing.assert_close(shaded.reshape(-1, 4)[:, :3], expect, rtol=2e-4, atol=1e-7)
+
+
+def model_test_view_queries(rb, sun_theta_deg, width=64, height=36):
+    """The view of atmosphere/reference/model_test.cc:436-477 (camera at
+    (2000, -8000, 500) m above a planet centred at (0, 0, -Rb), pitch pi/30,
+    50 degree vertical field of view, 640x360), sampled on a width x height
+    grid of pixel centres, with the sun at (theta, phi = 90 deg) (the test
+    cases' :812-1080).  Per pixel: the view ray; the point is the ground
+    point 1 m above the surface where the ray hits the planet, else 10 km
+    along the ray; the normal is the radial direction at the point."""
+    pitch = np.pi / 30.0
+    tan_fov = np.tan(np.radians(50.0) / 2.0)
+    aspect = 640.0 / 360.0
+    xs = (np.arange(width) + 0.5) / width * 2.0 - 1.0
+    ys = (np.arange(height) + 0.5) / height * 2.0 - 1.0
+    x, y = np.meshgrid(xs, ys)
+    vx, vy, vz = tan_fov * aspect * x, tan_fov * y, -np.ones_like(x)
+    # model_from_view rotation rows (1, 0, 0), (0, -sin p, -cos p), (0, cos p, -sin p).
+    view = np.stack([vx, -np.sin(pitch) * vy - np.cos(pitch) * vz,
+                     np.cos(pitch) * vy - np.sin(pitch) * vz], axis=-1).reshape(-1, 3)
+    view /= np.linalg.norm(view, axis=1, keepdims=True)
+    n = len(view)
+    cam = np.tile([2.0, -8.0, 0.5 + rb], (n, 1))
+    th = np.radians(sun_theta_deg)
+    sun = np.tile([0.0, np.sin(th), np.cos(th)], (n, 1))
+    rmu = np.sum(cam * view, axis=1)
+    disc = rmu * rmu - (np.sum(cam * cam, axis=1) - rb * rb)
+    t_ground = -rmu - np.sqrt(np.maximum(disc, 0.0))
+    ground = (disc >= 0.0) & (t_ground > 0.0)
+    point = cam + view * np.where(ground, t_ground, 10.0)[:, None]
+    normal = point / np.linalg.norm(point, axis=1, keepdims=True)
+    point = np.where(ground[:, None], normal * (rb + 1e-3), point)
+    shadow = np.zeros(n)
+    return as_f32((cam, view, sun, point, normal, shadow)), ground
+
+
+@pytest.mark.parametrize("combined", [True, False], ids=["combined", "separate"])
+@pytest.mark.parametrize("sun_theta", [65.0, 88.0])
+def test_model_test_view_vs_oracle(atmo, oracle, torch, sun_theta, combined):
+    """The render functions along the model_test view's pixel rays (sky
+    pixels and ground pixels) on the reference's default LUTs, against the
+    oracle's FP64 restatement of them, with the conditioning mask of
+    run_case."""
+    m = earth_model(atmo, combined=combined)
+    m.Init(4)
+    a = m.atmosphere_at()
+    S = m.scattering()
+    M = S if combined else m.single_mie_scattering()
+    q, ground = model_test_view_queries(a.bottom_radius, sun_theta)
+    assert 0.2 < ground.mean() < 0.8          # the horizon crosses the image
+    ref = OracleRender(oracle, a, atmo.DEFAULT_SHAPE, m.transmittance(), S, M,
+                       m.irradiance(), combined)
+    rng = np.random.default_rng(int(sun_theta))
+    ref_out = oracle_outputs(ref, q, rng, False)
+    # Positions move by ~0.5 m, FP32's own rounding of a coordinate at
+    # 6360 km (the random workload uses ~4x that).
+    pert_out = oracle_outputs(ref, q, rng, True, position=8e-8)
+    gpu_out = gpu_outputs(torch, m.lut_set(), q)
+    cam, _, sun, point, normal, _ = q
+    terms = np.array([ref.sky(cam[i], (point[i] - cam[i]) / np.linalg.norm(point[i] - cam[i]),
+                              0.0, sun[i])[0] for i in range(len(cam))])
+    factor = 0.5 * (1.0 + np.sum(normal * point, axis=1) / np.linalg.norm(point, axis=1))
+    # The camera is 500 m above the ground, where FP32 positions (~0.5 m at
+    # 6360 km) move the ground-side mu mapping of near-horizontal rays: fewer
+    # queries pass the conditioning mask than for the random workload.
+    compare(ref_out, pert_out, gpu_out, "model_test view, sun %g deg" % sun_theta, terms,
+            factor, min_robust=0.25)
