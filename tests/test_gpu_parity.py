@@ -94,6 +94,29 @@ def test_extreme_nu_sizes_vs_oracle(atmo, oracle, torch, nu, path):
 
 
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
+@pytest.mark.parametrize("orders", [1, 2, 12])
+def test_minimal_shape_vs_oracle(atmo, oracle, torch, orders, path):
+    """The smallest shape the C ABI accepts (every size 2, MU = 4: one texel
+    row per ray half, transmittance and irradiance of 2 x 2 texels), for one
+    order, two, and twelve (the long tail of many small orders)."""
+    shape = (2, 2, 2, 4, 2, 2, 2, 2)
+    atm = oracle.earth_atmosphere()
+    ref = oracle.precompute(atm, shape, orders, combined=False)
+    compare(ref, gpu_precompute(atmo, torch, atm, shape, orders, False, path), False)
+
+
+@pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
+def test_odd_sizes_vs_oracle(atmo, oracle, torch, path):
+    """Odd sizes everywhere but MU (which must be even): transmittance 33 x 9,
+    scattering R 5 x MU 14 x MU_S 5 x NU 3 (line width W = 15), irradiance
+    17 x 5."""
+    shape = (33, 9, 5, 14, 5, 3, 17, 5)
+    atm = oracle.earth_atmosphere()
+    ref = oracle.precompute(atm, shape, 4, combined=True)
+    compare(ref, gpu_precompute(atmo, torch, atm, shape, 4, True, path), True)
+
+
+@pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
 def test_medium_shape_random_atmospheres_vs_oracle(atmo, oracle, torch, path):
     """Non-Earth planets: seeded draws over the batched-rebuild ranges, compared
     on the texels where the FP64 reference is not rounding-dominated."""
