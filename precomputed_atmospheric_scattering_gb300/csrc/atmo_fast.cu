@@ -1,5 +1,7 @@
 // atmo_fast.cu -- fast-path kernels: the slab-restructured scattering density
-// (the dominant pass, functions.glsl:1163-1260) and the FP16 output conversion.
+// (the dominant pass, functions.glsl:1163-1260), the row-restructured single
+// and multiple scattering (:650-730, :1285-1330; described where they start
+// below), the FP16 output conversion and the FP32 FMA throughput probe.
 //
 // Scattering density, restructured.  For a texel at r-slice k and mu_s column
 // c, every incoming-radiance lookup of ComputeScatteringDensity is made at the
