@@ -212,8 +212,10 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
-  // the outgoing direction; nu1 differs by the sign of sy sin(phi).
-#pragma unroll 2
+  // the outgoing direction; nu1 differs by the sign of sy sin(phi).  Unrolled
+  // 4 times above order 2, not at order 2 (measured: -1.7% and -1.2%
+  // against 2).
+#pragma unroll(kOrder2 ? 1 : 4)
   for (int m = 0; m < kDensityPhiSamples / 2; ++m) {
     const float2 cs = c_density_phi[m];
     // Phase functions at nu2 (functions.glsl:739-747, :1245-1254), folded
