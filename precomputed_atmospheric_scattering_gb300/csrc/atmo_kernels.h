@@ -17,8 +17,10 @@ cudaError_t LaunchSingleScattering(const Instance* insts, WorkList wl, int tiles
                                    cudaStream_t st);
 cudaError_t LaunchDensityPlain(const Instance* insts, WorkList wl, int tiles, int order,
                                cudaStream_t st);
+// smem_bytes: IndirectSmem of the launch (0 on the plain path).
+int IndirectSmem(const Shape& s, int order);
 cudaError_t LaunchIndirectIrradiance(const Instance* insts, WorkList wl, int tiles, int order,
-                                     cudaStream_t st);
+                                     int smem_bytes, cudaStream_t st);
 cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
                                 cudaStream_t st);
 // Fast path (atmo_fast.cu).

@@ -132,6 +132,7 @@ int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path) {
   if (pass == Pass::kDensity) return DensityFastSmem(s, order);
   if (pass == Pass::kMultiple) return MultipleFastSmem(s);
   if (pass == Pass::kSingle) return SingleFastSmem(s);
+  if (pass == Pass::kIndirect) return IndirectSmem(s, order);
   return 0;
 }
 
@@ -306,7 +307,8 @@ cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, Wo
     case Pass::kDensity:
       return path == ATMO_PATH_FAST ? LaunchDensityFast(insts, wl, tiles, order, smem, st)
                                     : LaunchDensityPlain(insts, wl, tiles, order, st);
-    case Pass::kIndirect: return LaunchIndirectIrradiance(insts, wl, tiles, order, st);
+    case Pass::kIndirect:
+      return LaunchIndirectIrradiance(insts, wl, tiles, order, smem, st);
     case Pass::kMultiple:
       return path == ATMO_PATH_FAST ? LaunchMultipleFast(insts, wl, tiles, smem, st)
                                     : LaunchMultiplePlain(insts, wl, tiles, st);
