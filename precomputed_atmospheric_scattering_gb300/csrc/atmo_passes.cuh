@@ -120,6 +120,14 @@ ATMO_PASS float ProfileDensity64(const ProfileF& p, double h) {
                                       : LayerDensity(p.layer[1], (float)h);
 }
 
+// ProfileDensity for the optical-length samples: a layer without an
+// exponential term (the ozone layers) skips its exp (its product with 0).
+ATMO_PASS float SampleDensity(const ProfileF& p, float h) {
+  const LayerF& l = h < p.layer[0].width ? p.layer[0] : p.layer[1];
+  const float e = l.exp_term == 0.0f ? 0.0f : l.exp_term * expf(l.exp_scale * h);
+  return clampf(e + l.linear_term * h + l.constant_term, 0.0f, 1.0f);
+}
+
 ATMO_PASS void OpticalLengthPartial(const Consts& c, const TransmittanceRay& ray, int first,
                                     int stride, float out[3]) {
   Kahan kr, km, ka;
@@ -141,9 +149,9 @@ ATMO_PASS void OpticalLengthPartial(const Consts& c, const TransmittanceRay& ray
       ka.add(ProfileDensity64(c.prof_a, h) * w);
       continue;
     }
-    kr.add(ProfileDensity(c.prof_r, p.h) * w);
-    km.add(ProfileDensity(c.prof_m, p.h) * w);
-    ka.add(ProfileDensity(c.prof_a, p.h) * w);
+    kr.add(SampleDensity(c.prof_r, p.h) * w);
+    km.add(SampleDensity(c.prof_m, p.h) * w);
+    ka.add(SampleDensity(c.prof_a, p.h) * w);
   }
   out[0] = kr.s;
   out[1] = km.s;
