@@ -70,6 +70,10 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--warm-seconds", type=float, default=8.0,
+                   help="keep running untimed steps (at least --warmup) until the GPU has "
+                        "been busy this long: a GPU that starts idle runs the L1-bound "
+                        "kernels ~3%% slower for its first seconds")
     p.add_argument("--batch", type=int, default=16, help="atmospheres per batched step")
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -242,8 +246,12 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     # --- device-timed batched rebuilds -------------------------------------
-    for _ in range(args.warmup):
+    t_warm, warm_steps = time.perf_counter(), 0
+    while warm_steps < args.warmup or time.perf_counter() - t_warm < args.warm_seconds:
         batch.run(stream)
+        torch.cuda.synchronize()
+        warm_steps += 1
+    warm_s = time.perf_counter() - t_warm
     barrier()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clocks:
@@ -346,7 +354,8 @@ def run_gpu(args):
                    "parallelism": "replicas (independent batches "
                    "per GPU)" if world > 1 else "single GPU",
                    "l2": "no flush: each step's working set (%d MB) exceeds the 129 MB L2"
-                         % (B * 64)},
+                         % (B * 64),
+                   "warm_up": {"steps": warm_steps, "seconds": round(warm_s, 2)}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "single_rebuild": {"p50_ms": p50, "p99_ms": p99, "fast_rebuilds_per_s": 1000.0 / p50,
