@@ -24,7 +24,9 @@ def main():
     b = Batch([W.earth() for _ in range(a.batch)], [SHAPES[a.shape]] * a.batch, a.orders)
     if a.no_graph:
         for _ in range(a.runs):
-            b.time_passes()
+            passes = b.time_passes()
+        for name, order, ms in passes:
+            print("%-22s %2d %9.4f ms" % (name, order, ms))
     else:
         for _ in range(a.runs):
             b.run()
