@@ -21,63 +21,86 @@
 #include <thread>
 #include <vector>
 
+#if defined(__CUDACC__)
+#define ORACLE_HD __host__ __device__
+#else
+#define ORACLE_HD
+#endif
+
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
+
+// The math of the texel evaluators, callable from host and (in the FP64 GPU
+// build, atmo_oracle_gpu.cu) device code: the C library functions, and
+// min / max with the std:: semantics.
+namespace om {
+ORACLE_HD inline double sqrt(double x) { return ::sqrt(x); }
+ORACLE_HD inline double exp(double x) { return ::exp(x); }
+ORACLE_HD inline double floor(double x) { return ::floor(x); }
+ORACLE_HD inline double fmod(double x, double y) { return ::fmod(x, y); }
+ORACLE_HD inline double pow(double x, double y) { return ::pow(x, y); }
+ORACLE_HD inline double sin(double x) { return ::sin(x); }
+ORACLE_HD inline double cos(double x) { return ::cos(x); }
+template <class T>
+ORACLE_HD inline T min(T a, T b) { return b < a ? b : a; }
+template <class T>
+ORACLE_HD inline T max(T a, T b) { return a < b ? b : a; }
+}  // namespace om
 
 // ---------------------------------------------------------------------------
 // Small vector types (the GLSL vec3 / spectrum of atmosphere/definitions.glsl)
 // ---------------------------------------------------------------------------
 struct Spec {
   double v[3];
-  Spec() : v{0, 0, 0} {}
-  explicit Spec(double a) : v{a, a, a} {}
-  Spec(double a, double b, double c) : v{a, b, c} {}
-  static Spec From(const double* p) { return Spec(p[0], p[1], p[2]); }
-  double& operator[](int i) { return v[i]; }
-  double operator[](int i) const { return v[i]; }
+  ORACLE_HD Spec() : v{0, 0, 0} {}
+  ORACLE_HD explicit Spec(double a) : v{a, a, a} {}
+  ORACLE_HD Spec(double a, double b, double c) : v{a, b, c} {}
+  ORACLE_HD static Spec From(const double* p) { return Spec(p[0], p[1], p[2]); }
+  ORACLE_HD double& operator[](int i) { return v[i]; }
+  ORACLE_HD double operator[](int i) const { return v[i]; }
 };
-inline Spec operator+(const Spec& a, const Spec& b) {
+ORACLE_HD inline Spec operator+(const Spec& a, const Spec& b) {
   return Spec(a[0] + b[0], a[1] + b[1], a[2] + b[2]);
 }
-inline Spec operator-(const Spec& a, const Spec& b) {
+ORACLE_HD inline Spec operator-(const Spec& a, const Spec& b) {
   return Spec(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
 }
-inline Spec operator*(const Spec& a, const Spec& b) {
+ORACLE_HD inline Spec operator*(const Spec& a, const Spec& b) {
   return Spec(a[0] * b[0], a[1] * b[1], a[2] * b[2]);
 }
-inline Spec operator/(const Spec& a, const Spec& b) {
+ORACLE_HD inline Spec operator/(const Spec& a, const Spec& b) {
   return Spec(a[0] / b[0], a[1] / b[1], a[2] / b[2]);
 }
-inline Spec operator*(const Spec& a, double s) {
+ORACLE_HD inline Spec operator*(const Spec& a, double s) {
   return Spec(a[0] * s, a[1] * s, a[2] * s);
 }
-inline Spec operator*(double s, const Spec& a) { return a * s; }
-inline Spec operator/(const Spec& a, double s) {
+ORACLE_HD inline Spec operator*(double s, const Spec& a) { return a * s; }
+ORACLE_HD inline Spec operator/(const Spec& a, double s) {
   return Spec(a[0] / s, a[1] / s, a[2] / s);
 }
-inline Spec& operator+=(Spec& a, const Spec& b) { return a = a + b; }
-inline Spec sexp(const Spec& a) {
-  return Spec(std::exp(a[0]), std::exp(a[1]), std::exp(a[2]));
+ORACLE_HD inline Spec& operator+=(Spec& a, const Spec& b) { return a = a + b; }
+ORACLE_HD inline Spec sexp(const Spec& a) {
+  return Spec(om::exp(a[0]), om::exp(a[1]), om::exp(a[2]));
 }
-inline Spec smin(const Spec& a, const Spec& b) {
-  return Spec(std::min(a[0], b[0]), std::min(a[1], b[1]), std::min(a[2], b[2]));
+ORACLE_HD inline Spec smin(const Spec& a, const Spec& b) {
+  return Spec(om::min(a[0], b[0]), om::min(a[1], b[1]), om::min(a[2], b[2]));
 }
 
 struct V3 {
   double x, y, z;
 };
-inline V3 operator+(const V3& a, const V3& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline V3 operator-(const V3& a, const V3& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline V3 operator*(const V3& a, double s) { return {a.x * s, a.y * s, a.z * s}; }
-inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline double length(const V3& a) { return std::sqrt(dot(a, a)); }
-inline V3 normalize(const V3& a) { return a * (1.0 / length(a)); }
+ORACLE_HD inline V3 operator+(const V3& a, const V3& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+ORACLE_HD inline V3 operator-(const V3& a, const V3& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+ORACLE_HD inline V3 operator*(const V3& a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+ORACLE_HD inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+ORACLE_HD inline double length(const V3& a) { return om::sqrt(dot(a, a)); }
+ORACLE_HD inline V3 normalize(const V3& a) { return a * (1.0 / length(a)); }
 
-inline double clampd(double x, double lo, double hi) { return std::min(std::max(x, lo), hi); }
+ORACLE_HD inline double clampd(double x, double lo, double hi) { return om::min(om::max(x, lo), hi); }
 // GLSL smoothstep; for the degenerate e0 == e1 (a point sun) it returns 0 at
 // x <= e0 and 1 above, where the clamp formula would give 0/0.
-inline double smoothstep(double e0, double e1, double x) {
+ORACLE_HD inline double smoothstep(double e0, double e1, double x) {
   if (x <= e0) return 0.0;
   if (x >= e1) return 1.0;
   double t = (x - e0) / (e1 - e0);
@@ -90,35 +113,35 @@ inline double smoothstep(double e0, double e1, double x) {
 struct Tex2 {
   int w = 0, h = 0;
   const double* p = nullptr;  // RGBA
-  Spec Get(int i, int j) const {
-    i = std::min(std::max(i, 0), w - 1);
-    j = std::min(std::max(j, 0), h - 1);
+  ORACLE_HD Spec Get(int i, int j) const {
+    i = om::min(om::max(i, 0), w - 1);
+    j = om::min(om::max(j, 0), h - 1);
     return Spec::From(p + 4 * ((long long)j * w + i));
   }
 };
 struct Tex3 {
   int w = 0, h = 0, d = 0;
   const double* p = nullptr;  // RGBA
-  Spec Get(int i, int j, int k) const {
-    i = std::min(std::max(i, 0), w - 1);
-    j = std::min(std::max(j, 0), h - 1);
-    k = std::min(std::max(k, 0), d - 1);
+  ORACLE_HD Spec Get(int i, int j, int k) const {
+    i = om::min(om::max(i, 0), w - 1);
+    j = om::min(om::max(j, 0), h - 1);
+    k = om::min(om::max(k, 0), d - 1);
     return Spec::From(p + 4 * (((long long)k * h + j) * w + i));
   }
 };
 
-Spec texture(const Tex2& t, double u, double v) {
+ORACLE_HD Spec texture(const Tex2& t, double u, double v) {
   double x = u * t.w - 0.5, y = v * t.h - 0.5;
-  double fi = std::floor(x), fj = std::floor(y);
+  double fi = om::floor(x), fj = om::floor(y);
   int i = (int)fi, j = (int)fj;
   double a = x - fi, b = y - fj;
   return t.Get(i, j) * ((1.0 - a) * (1.0 - b)) + t.Get(i + 1, j) * (a * (1.0 - b)) +
          t.Get(i, j + 1) * ((1.0 - a) * b) + t.Get(i + 1, j + 1) * (a * b);
 }
 
-Spec texture(const Tex3& t, double u, double v, double w) {
+ORACLE_HD Spec texture(const Tex3& t, double u, double v, double w) {
   double x = u * t.w - 0.5, y = v * t.h - 0.5, z = w * t.d - 0.5;
-  double fi = std::floor(x), fj = std::floor(y), fk = std::floor(z);
+  double fi = om::floor(x), fj = om::floor(y), fk = om::floor(z);
   int i = (int)fi, j = (int)fj, k = (int)fk;
   double a = x - fi, b = y - fj, c = z - fk;
   Spec r;
@@ -132,18 +155,18 @@ Spec texture(const Tex3& t, double u, double v, double w) {
 }
 
 // Texel taps (clamped flat indices and weights) of the 3D lookup above.
-void texture_taps(const Tex3& t, double u, double v, double w, int idx[8], double wt[8]) {
+ORACLE_HD void texture_taps(const Tex3& t, double u, double v, double w, int idx[8], double wt[8]) {
   double x = u * t.w - 0.5, y = v * t.h - 0.5, z = w * t.d - 0.5;
-  double fi = std::floor(x), fj = std::floor(y), fk = std::floor(z);
+  double fi = om::floor(x), fj = om::floor(y), fk = om::floor(z);
   int i = (int)fi, j = (int)fj, k = (int)fk;
   double a = x - fi, b = y - fj, c = z - fk;
   int n = 0;
   for (int dk = 0; dk < 2; ++dk)
     for (int dj = 0; dj < 2; ++dj)
       for (int di = 0; di < 2; ++di) {
-        int ii = std::min(std::max(i + di, 0), t.w - 1);
-        int jj = std::min(std::max(j + dj, 0), t.h - 1);
-        int kk = std::min(std::max(k + dk, 0), t.d - 1);
+        int ii = om::min(om::max(i + di, 0), t.w - 1);
+        int jj = om::min(om::max(j + dj, 0), t.h - 1);
+        int kk = om::min(om::max(k + dk, 0), t.d - 1);
         idx[n] = (kk * t.h + jj) * t.w + ii;
         wt[n] = (di ? a : 1.0 - a) * (dj ? b : 1.0 - b) * (dk ? c : 1.0 - c);
         ++n;
@@ -174,7 +197,7 @@ struct Atm {
   int T_W, T_H, S_R, S_MU, S_MU_S, S_NU, I_W, I_H;
 };
 
-Profile ToProfile(const oracle_profile& p) {
+ORACLE_HD Profile ToProfile(const oracle_profile& p) {
   Profile q;
   for (int i = 0; i < 2; ++i) {
     q.layers[i] = {p.layers[i].width, p.layers[i].exp_term, p.layers[i].exp_scale,
@@ -183,7 +206,7 @@ Profile ToProfile(const oracle_profile& p) {
   return q;
 }
 
-Atm ToAtm(const oracle_atmosphere* a, const oracle_shape* s) {
+ORACLE_HD Atm ToAtm(const oracle_atmosphere* a, const oracle_shape* s) {
   Atm t;
   t.solar_irradiance = Spec::From(a->solar_irradiance);
   t.sun_angular_radius = a->sun_angular_radius;
@@ -215,51 +238,51 @@ Atm ToAtm(const oracle_atmosphere* a, const oracle_shape* s) {
   return t;
 }
 
-Tex2 MakeT(const Atm& a, const double* p) { return Tex2{a.T_W, a.T_H, p}; }
-Tex2 MakeI(const Atm& a, const double* p) { return Tex2{a.I_W, a.I_H, p}; }
-Tex3 MakeS(const Atm& a, const double* p) {
+ORACLE_HD Tex2 MakeT(const Atm& a, const double* p) { return Tex2{a.T_W, a.T_H, p}; }
+ORACLE_HD Tex2 MakeI(const Atm& a, const double* p) { return Tex2{a.I_W, a.I_H, p}; }
+ORACLE_HD Tex3 MakeS(const Atm& a, const double* p) {
   return Tex3{a.S_NU * a.S_MU_S, a.S_MU, a.S_R, p};
 }
 
 // functions.glsl:113-127
-double ClampCosine(double mu) { return clampd(mu, -1.0, 1.0); }
-double ClampDistance(double d) { return std::max(d, 0.0); }
-double ClampRadius(const Atm& a, double r) { return clampd(r, a.bottom_radius, a.top_radius); }
-double SafeSqrt(double x) { return std::sqrt(std::max(x, 0.0)); }
+ORACLE_HD double ClampCosine(double mu) { return clampd(mu, -1.0, 1.0); }
+ORACLE_HD double ClampDistance(double d) { return om::max(d, 0.0); }
+ORACLE_HD double ClampRadius(const Atm& a, double r) { return clampd(r, a.bottom_radius, a.top_radius); }
+ORACLE_HD double SafeSqrt(double x) { return om::sqrt(om::max(x, 0.0)); }
 
 // functions.glsl:207-214
-double DistanceToTopAtmosphereBoundary(const Atm& a, double r, double mu) {
+ORACLE_HD double DistanceToTopAtmosphereBoundary(const Atm& a, double r, double mu) {
   double discriminant = r * r * (mu * mu - 1.0) + a.top_radius * a.top_radius;
   return ClampDistance(-r * mu + SafeSqrt(discriminant));
 }
 // functions.glsl:222-229
-double DistanceToBottomAtmosphereBoundary(const Atm& a, double r, double mu) {
+ORACLE_HD double DistanceToBottomAtmosphereBoundary(const Atm& a, double r, double mu) {
   double discriminant = r * r * (mu * mu - 1.0) + a.bottom_radius * a.bottom_radius;
   return ClampDistance(-r * mu - SafeSqrt(discriminant));
 }
 // functions.glsl:240-246
-bool RayIntersectsGround(const Atm& a, double r, double mu) {
+ORACLE_HD bool RayIntersectsGround(const Atm& a, double r, double mu) {
   return mu < 0.0 && r * r * (mu * mu - 1.0) + a.bottom_radius * a.bottom_radius >= 0.0;
 }
 // functions.glsl:263-273
-double GetLayerDensity(const Layer& l, double altitude) {
-  double density = l.exp_term * std::exp(l.exp_scale * altitude) +
+ORACLE_HD double GetLayerDensity(const Layer& l, double altitude) {
+  double density = l.exp_term * om::exp(l.exp_scale * altitude) +
                    l.linear_term * altitude + l.constant_term;
   return clampd(density, 0.0, 1.0);
 }
-double GetProfileDensity(const Profile& p, double altitude) {
+ORACLE_HD double GetProfileDensity(const Profile& p, double altitude) {
   return altitude < p.layers[0].width ? GetLayerDensity(p.layers[0], altitude)
                                       : GetLayerDensity(p.layers[1], altitude);
 }
 // functions.glsl:275-299 (500 intervals, trapezoidal rule)
-double ComputeOpticalLengthToTopAtmosphereBoundary(const Atm& a, const Profile& p, double r,
+ORACLE_HD double ComputeOpticalLengthToTopAtmosphereBoundary(const Atm& a, const Profile& p, double r,
                                                    double mu) {
   const int SAMPLE_COUNT = 500;
   double dx = DistanceToTopAtmosphereBoundary(a, r, mu) / double(SAMPLE_COUNT);
   double result = 0.0;
   for (int i = 0; i <= SAMPLE_COUNT; ++i) {
     double d_i = double(i) * dx;
-    double r_i = std::sqrt(d_i * d_i + 2.0 * r * mu * d_i + r * r);
+    double r_i = om::sqrt(d_i * d_i + 2.0 * r * mu * d_i + r * r);
     double y_i = GetProfileDensity(p, r_i - a.bottom_radius);
     double weight_i = i == 0 || i == SAMPLE_COUNT ? 0.5 : 1.0;
     result += y_i * weight_i * dx;
@@ -267,7 +290,7 @@ double ComputeOpticalLengthToTopAtmosphereBoundary(const Atm& a, const Profile& 
   return result;
 }
 // functions.glsl:306-320
-Spec ComputeTransmittanceToTopAtmosphereBoundary(const Atm& a, double r, double mu) {
+ORACLE_HD Spec ComputeTransmittanceToTopAtmosphereBoundary(const Atm& a, double r, double mu) {
   return sexp(Spec(0.0) -
               (a.rayleigh_scattering *
                    ComputeOpticalLengthToTopAtmosphereBoundary(a, a.rayleigh_density, r, mu) +
@@ -277,16 +300,16 @@ Spec ComputeTransmittanceToTopAtmosphereBoundary(const Atm& a, double r, double 
                                              a, a.absorption_density, r, mu)));
 }
 // functions.glsl:342-348
-double GetTextureCoordFromUnitRange(double x, int n) {
+ORACLE_HD double GetTextureCoordFromUnitRange(double x, int n) {
   return 0.5 / double(n) + x * (1.0 - 1.0 / double(n));
 }
-double GetUnitRangeFromTextureCoord(double u, int n) {
+ORACLE_HD double GetUnitRangeFromTextureCoord(double u, int n) {
   return (u - 0.5 / double(n)) / (1.0 - 1.0 / double(n));
 }
 // functions.glsl:402-421
-void GetTransmittanceTextureUvFromRMu(const Atm& a, double r, double mu, double* u,
+ORACLE_HD void GetTransmittanceTextureUvFromRMu(const Atm& a, double r, double mu, double* u,
                                       double* v) {
-  double H = std::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
+  double H = om::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
   double rho = SafeSqrt(r * r - a.bottom_radius * a.bottom_radius);
   double d = DistanceToTopAtmosphereBoundary(a, r, mu);
   double d_min = a.top_radius - r;
@@ -297,13 +320,13 @@ void GetTransmittanceTextureUvFromRMu(const Atm& a, double r, double mu, double*
   *v = GetTextureCoordFromUnitRange(x_r, a.T_H);
 }
 // functions.glsl:427-448
-void GetRMuFromTransmittanceTextureUv(const Atm& a, double u, double v, double* r,
+ORACLE_HD void GetRMuFromTransmittanceTextureUv(const Atm& a, double u, double v, double* r,
                                       double* mu) {
   double x_mu = GetUnitRangeFromTextureCoord(u, a.T_W);
   double x_r = GetUnitRangeFromTextureCoord(v, a.T_H);
-  double H = std::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
+  double H = om::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
   double rho = H * x_r;
-  *r = std::sqrt(rho * rho + a.bottom_radius * a.bottom_radius);
+  *r = om::sqrt(rho * rho + a.bottom_radius * a.bottom_radius);
   double d_min = a.top_radius - *r;
   double d_max = rho + H;
   double d = d_min + x_mu * (d_max - d_min);
@@ -311,22 +334,22 @@ void GetRMuFromTransmittanceTextureUv(const Atm& a, double u, double v, double* 
   *mu = ClampCosine(m);
 }
 // functions.glsl:454-463
-Spec ComputeTransmittanceToTopAtmosphereBoundaryTexture(const Atm& a, double fx, double fy) {
+ORACLE_HD Spec ComputeTransmittanceToTopAtmosphereBoundaryTexture(const Atm& a, double fx, double fy) {
   double r, mu;
   GetRMuFromTransmittanceTextureUv(a, fx / a.T_W, fy / a.T_H, &r, &mu);
   return ComputeTransmittanceToTopAtmosphereBoundary(a, r, mu);
 }
 // functions.glsl:473-480
-Spec GetTransmittanceToTopAtmosphereBoundary(const Atm& a, const Tex2& T, double r,
+ORACLE_HD Spec GetTransmittanceToTopAtmosphereBoundary(const Atm& a, const Tex2& T, double r,
                                              double mu) {
   double u, v;
   GetTransmittanceTextureUvFromRMu(a, r, mu, &u, &v);
   return texture(T, u, v);
 }
 // functions.glsl:493-515
-Spec GetTransmittance(const Atm& a, const Tex2& T, double r, double mu, double d,
+ORACLE_HD Spec GetTransmittance(const Atm& a, const Tex2& T, double r, double mu, double d,
                       bool ray_r_mu_intersects_ground) {
-  double r_d = ClampRadius(a, std::sqrt(d * d + 2.0 * r * mu * d + r * r));
+  double r_d = ClampRadius(a, om::sqrt(d * d + 2.0 * r * mu * d + r * r));
   double mu_d = ClampCosine((r * mu + d) / r_d);
   if (ray_r_mu_intersects_ground) {
     return smin(GetTransmittanceToTopAtmosphereBoundary(a, T, r_d, -mu_d) /
@@ -339,19 +362,19 @@ Spec GetTransmittance(const Atm& a, const Tex2& T, double r, double mu, double d
   }
 }
 // functions.glsl:552-563
-Spec GetTransmittanceToSun(const Atm& a, const Tex2& T, double r, double mu_s) {
+ORACLE_HD Spec GetTransmittanceToSun(const Atm& a, const Tex2& T, double r, double mu_s) {
   double sin_theta_h = a.bottom_radius / r;
-  double cos_theta_h = -std::sqrt(std::max(1.0 - sin_theta_h * sin_theta_h, 0.0));
+  double cos_theta_h = -om::sqrt(om::max(1.0 - sin_theta_h * sin_theta_h, 0.0));
   return GetTransmittanceToTopAtmosphereBoundary(a, T, r, mu_s) *
          smoothstep(-sin_theta_h * a.sun_angular_radius, sin_theta_h * a.sun_angular_radius,
                     mu_s - cos_theta_h);
 }
 // functions.glsl:650-667
-void ComputeSingleScatteringIntegrand(const Atm& a, const Tex2& T, double r, double mu,
+ORACLE_HD void ComputeSingleScatteringIntegrand(const Atm& a, const Tex2& T, double r, double mu,
                                       double mu_s, double nu, double d,
                                       bool ray_r_mu_intersects_ground, Spec* rayleigh,
                                       Spec* mie) {
-  double r_d = ClampRadius(a, std::sqrt(d * d + 2.0 * r * mu * d + r * r));
+  double r_d = ClampRadius(a, om::sqrt(d * d + 2.0 * r * mu * d + r * r));
   double mu_s_d = ClampCosine((r * mu_s + d * nu) / r_d);
   Spec transmittance = GetTransmittance(a, T, r, mu, d, ray_r_mu_intersects_ground) *
                        GetTransmittanceToSun(a, T, r_d, mu_s_d);
@@ -359,13 +382,13 @@ void ComputeSingleScatteringIntegrand(const Atm& a, const Tex2& T, double r, dou
   *mie = transmittance * GetProfileDensity(a.mie_density, r_d - a.bottom_radius);
 }
 // functions.glsl:680-687
-double DistanceToNearestAtmosphereBoundary(const Atm& a, double r, double mu,
+ORACLE_HD double DistanceToNearestAtmosphereBoundary(const Atm& a, double r, double mu,
                                            bool ray_r_mu_intersects_ground) {
   return ray_r_mu_intersects_ground ? DistanceToBottomAtmosphereBoundary(a, r, mu)
                                     : DistanceToTopAtmosphereBoundary(a, r, mu);
 }
 // functions.glsl:695-730 (50 intervals)
-void ComputeSingleScattering(const Atm& a, const Tex2& T, double r, double mu, double mu_s,
+ORACLE_HD void ComputeSingleScattering(const Atm& a, const Tex2& T, double r, double mu, double mu_s,
                              double nu, bool ray_r_mu_intersects_ground, Spec* rayleigh,
                              Spec* mie) {
   const int SAMPLE_COUNT = 50;
@@ -385,19 +408,19 @@ void ComputeSingleScattering(const Atm& a, const Tex2& T, double r, double mu, d
   *mie = mie_sum * dx * a.solar_irradiance * a.mie_scattering;
 }
 // functions.glsl:739-747
-double RayleighPhaseFunction(double nu) {
+ORACLE_HD double RayleighPhaseFunction(double nu) {
   double k = 3.0 / (16.0 * kPi);
   return k * (1.0 + nu * nu);
 }
-double MiePhaseFunction(double g, double nu) {
+ORACLE_HD double MiePhaseFunction(double g, double nu) {
   double k = 3.0 / (8.0 * kPi) * (1.0 - g * g) / (2.0 + g * g);
-  return k * (1.0 + nu * nu) / std::pow(1.0 + g * g - 2.0 * g * nu, 1.5);
+  return k * (1.0 + nu * nu) / om::pow(1.0 + g * g - 2.0 * g * nu, 1.5);
 }
 // functions.glsl:773-831
-void GetScatteringTextureUvwzFromRMuMuSNu(const Atm& a, double r, double mu, double mu_s,
+ORACLE_HD void GetScatteringTextureUvwzFromRMuMuSNu(const Atm& a, double r, double mu, double mu_s,
                                           double nu, bool ray_r_mu_intersects_ground,
                                           double uvwz[4]) {
-  double H = std::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
+  double H = om::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
   double rho = SafeSqrt(r * r - a.bottom_radius * a.bottom_radius);
   double u_r = GetTextureCoordFromUnitRange(rho / H, a.S_R);
   double r_mu = r * mu;
@@ -422,7 +445,7 @@ void GetScatteringTextureUvwzFromRMuMuSNu(const Atm& a, double r, double mu, dou
   double D = DistanceToTopAtmosphereBoundary(a, a.bottom_radius, a.mu_s_min);
   double A = (D - d_min) / (d_max - d_min);
   double u_mu_s =
-      GetTextureCoordFromUnitRange(std::max(1.0 - aa / A, 0.0) / (1.0 + aa), a.S_MU_S);
+      GetTextureCoordFromUnitRange(om::max(1.0 - aa / A, 0.0) / (1.0 + aa), a.S_MU_S);
   double u_nu = (nu + 1.0) / 2.0;
   uvwz[0] = u_nu;
   uvwz[1] = u_mu_s;
@@ -430,12 +453,12 @@ void GetScatteringTextureUvwzFromRMuMuSNu(const Atm& a, double r, double mu, dou
   uvwz[3] = u_r;
 }
 // functions.glsl:837-890
-void GetRMuMuSNuFromScatteringTextureUvwz(const Atm& a, const double uvwz[4], double* r,
+ORACLE_HD void GetRMuMuSNuFromScatteringTextureUvwz(const Atm& a, const double uvwz[4], double* r,
                                           double* mu, double* mu_s, double* nu,
                                           bool* ray_r_mu_intersects_ground) {
-  double H = std::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
+  double H = om::sqrt(a.top_radius * a.top_radius - a.bottom_radius * a.bottom_radius);
   double rho = H * GetUnitRangeFromTextureCoord(uvwz[3], a.S_R);
-  *r = std::sqrt(rho * rho + a.bottom_radius * a.bottom_radius);
+  *r = om::sqrt(rho * rho + a.bottom_radius * a.bottom_radius);
   if (uvwz[2] < 0.5) {
     double d_min = *r - a.bottom_radius;
     double d_max = rho;
@@ -457,30 +480,30 @@ void GetRMuMuSNuFromScatteringTextureUvwz(const Atm& a, const double uvwz[4], do
   double D = DistanceToTopAtmosphereBoundary(a, a.bottom_radius, a.mu_s_min);
   double A = (D - d_min) / (d_max - d_min);
   double aa = (A - x_mu_s * A) / (1.0 + x_mu_s * A);
-  double d = d_min + std::min(aa, A) * (d_max - d_min);
+  double d = d_min + om::min(aa, A) * (d_max - d_min);
   *mu_s = d == 0.0 ? 1.0 : ClampCosine((H * H - d * d) / (2.0 * a.bottom_radius * d));
   *nu = ClampCosine(uvwz[0] * 2.0 - 1.0);
 }
 // functions.glsl:905-926
-void GetRMuMuSNuFromScatteringTextureFragCoord(const Atm& a, double fx, double fy,
+ORACLE_HD void GetRMuMuSNuFromScatteringTextureFragCoord(const Atm& a, double fx, double fy,
                                                double fz, double* r, double* mu,
                                                double* mu_s, double* nu,
                                                bool* ray_r_mu_intersects_ground) {
-  double frag_coord_nu = std::floor(fx / double(a.S_MU_S));
-  double frag_coord_mu_s = std::fmod(fx, double(a.S_MU_S));
+  double frag_coord_nu = om::floor(fx / double(a.S_MU_S));
+  double frag_coord_mu_s = om::fmod(fx, double(a.S_MU_S));
   double uvwz[4] = {frag_coord_nu / double(a.S_NU - 1), frag_coord_mu_s / double(a.S_MU_S),
                     fy / double(a.S_MU), fz / double(a.S_R)};
   GetRMuMuSNuFromScatteringTextureUvwz(a, uvwz, r, mu, mu_s, nu, ray_r_mu_intersects_ground);
-  *nu = clampd(*nu, *mu * *mu_s - std::sqrt((1.0 - *mu * *mu) * (1.0 - *mu_s * *mu_s)),
-               *mu * *mu_s + std::sqrt((1.0 - *mu * *mu) * (1.0 - *mu_s * *mu_s)));
+  *nu = clampd(*nu, *mu * *mu_s - om::sqrt((1.0 - *mu * *mu) * (1.0 - *mu_s * *mu_s)),
+               *mu * *mu_s + om::sqrt((1.0 - *mu * *mu) * (1.0 - *mu_s * *mu_s)));
 }
 // functions.glsl:958-976: two trilinear lookups lerped in nu.
-void ScatteringLookupCoords(const Atm& a, double r, double mu, double mu_s, double nu,
+ORACLE_HD void ScatteringLookupCoords(const Atm& a, double r, double mu, double mu_s, double nu,
                             bool ground, double uvw0[3], double uvw1[3], double* lerp) {
   double uvwz[4];
   GetScatteringTextureUvwzFromRMuMuSNu(a, r, mu, mu_s, nu, ground, uvwz);
   double tex_coord_x = uvwz[0] * double(a.S_NU - 1);
-  double tex_x = std::floor(tex_coord_x);
+  double tex_x = om::floor(tex_coord_x);
   *lerp = tex_coord_x - tex_x;
   uvw0[0] = (tex_x + uvwz[1]) / double(a.S_NU);
   uvw0[1] = uvwz[2];
@@ -489,7 +512,7 @@ void ScatteringLookupCoords(const Atm& a, double r, double mu, double mu_s, doub
   uvw1[1] = uvwz[2];
   uvw1[2] = uvwz[3];
 }
-Spec GetScattering(const Atm& a, const Tex3& S, double r, double mu, double mu_s, double nu,
+ORACLE_HD Spec GetScattering(const Atm& a, const Tex3& S, double r, double mu, double mu_s, double nu,
                    bool ground) {
   double uvw0[3], uvw1[3], lerp;
   ScatteringLookupCoords(a, r, mu, mu_s, nu, ground, uvw0, uvw1, &lerp);
@@ -497,7 +520,7 @@ Spec GetScattering(const Atm& a, const Tex3& S, double r, double mu, double mu_s
          texture(S, uvw1[0], uvw1[1], uvw1[2]) * lerp;
 }
 // functions.glsl:987-1009
-Spec GetScattering(const Atm& a, const Tex3& SR, const Tex3& SM, const Tex3& SMulti, double r,
+ORACLE_HD Spec GetScattering(const Atm& a, const Tex3& SR, const Tex3& SM, const Tex3& SMulti, double r,
                    double mu, double mu_s, double nu, bool ground, int scattering_order) {
   if (scattering_order == 1) {
     Spec rayleigh = GetScattering(a, SR, r, mu, mu_s, nu, ground);
@@ -508,7 +531,7 @@ Spec GetScattering(const Atm& a, const Tex3& SR, const Tex3& SM, const Tex3& SMu
   return GetScattering(a, SMulti, r, mu, mu_s, nu, ground);
 }
 // functions.glsl:1524-1533
-void GetIrradianceTextureUvFromRMuS(const Atm& a, double r, double mu_s, double* u,
+ORACLE_HD void GetIrradianceTextureUvFromRMuS(const Atm& a, double r, double mu_s, double* u,
                                     double* v) {
   double x_r = (r - a.bottom_radius) / (a.top_radius - a.bottom_radius);
   double x_mu_s = mu_s * 0.5 + 0.5;
@@ -516,7 +539,7 @@ void GetIrradianceTextureUvFromRMuS(const Atm& a, double r, double mu_s, double*
   *v = GetTextureCoordFromUnitRange(x_r, a.I_H);
 }
 // functions.glsl:1539-1548
-void GetRMuSFromIrradianceTextureUv(const Atm& a, double u, double v, double* r,
+ORACLE_HD void GetRMuSFromIrradianceTextureUv(const Atm& a, double u, double v, double* r,
                                     double* mu_s) {
   double x_mu_s = GetUnitRangeFromTextureCoord(u, a.I_W);
   double x_r = GetUnitRangeFromTextureCoord(v, a.I_H);
@@ -524,19 +547,19 @@ void GetRMuSFromIrradianceTextureUv(const Atm& a, double u, double v, double* r,
   *mu_s = ClampCosine(2.0 * x_mu_s - 1.0);
 }
 // functions.glsl:1595-1601
-Spec GetIrradiance(const Atm& a, const Tex2& I, double r, double mu_s) {
+ORACLE_HD Spec GetIrradiance(const Atm& a, const Tex2& I, double r, double mu_s) {
   double u, v;
   GetIrradianceTextureUvFromRMuS(a, r, mu_s, &u, &v);
   return texture(I, u, v);
 }
 // functions.glsl:1163-1260 (16 x 32 midpoint quadrature over the sphere)
-Spec ComputeScatteringDensity(const Atm& a, const Tex2& T, const Tex3& SR, const Tex3& SM,
+ORACLE_HD Spec ComputeScatteringDensity(const Atm& a, const Tex2& T, const Tex3& SR, const Tex3& SM,
                               const Tex3& SMulti, const Tex2& I, double r, double mu,
                               double mu_s, double nu, int scattering_order) {
   V3 zenith_direction{0.0, 0.0, 1.0};
-  V3 omega{std::sqrt(1.0 - mu * mu), 0.0, mu};
+  V3 omega{om::sqrt(1.0 - mu * mu), 0.0, mu};
   double sun_dir_x = omega.x == 0.0 ? 0.0 : (nu - mu * mu_s) / omega.x;
-  double sun_dir_y = std::sqrt(std::max(1.0 - sun_dir_x * sun_dir_x - mu_s * mu_s, 0.0));
+  double sun_dir_y = om::sqrt(om::max(1.0 - sun_dir_x * sun_dir_x - mu_s * mu_s, 0.0));
   V3 omega_s{sun_dir_x, sun_dir_y, mu_s};
   const int SAMPLE_COUNT = 16;
   const double dphi = kPi / double(SAMPLE_COUNT);
@@ -544,8 +567,8 @@ Spec ComputeScatteringDensity(const Atm& a, const Tex2& T, const Tex3& SR, const
   Spec rayleigh_mie;
   for (int l = 0; l < SAMPLE_COUNT; ++l) {
     double theta = (double(l) + 0.5) * dtheta;
-    double cos_theta = std::cos(theta);
-    double sin_theta = std::sin(theta);
+    double cos_theta = om::cos(theta);
+    double sin_theta = om::sin(theta);
     bool ray_r_theta_intersects_ground = RayIntersectsGround(a, r, cos_theta);
     double distance_to_ground = 0.0;
     Spec transmittance_to_ground(0.0);
@@ -557,8 +580,8 @@ Spec ComputeScatteringDensity(const Atm& a, const Tex2& T, const Tex3& SR, const
     }
     for (int m = 0; m < 2 * SAMPLE_COUNT; ++m) {
       double phi = (double(m) + 0.5) * dphi;
-      V3 omega_i{std::cos(phi) * sin_theta, std::sin(phi) * sin_theta, cos_theta};
-      double domega_i = dtheta * dphi * std::sin(theta);
+      V3 omega_i{om::cos(phi) * sin_theta, om::sin(phi) * sin_theta, cos_theta};
+      double domega_i = dtheta * dphi * om::sin(theta);
       double nu1 = dot(omega_s, omega_i);
       Spec incident_radiance = GetScattering(a, SR, SM, SMulti, r, omega_i.z, mu_s, nu1,
                                              ray_r_theta_intersects_ground,
@@ -582,7 +605,7 @@ Spec ComputeScatteringDensity(const Atm& a, const Tex2& T, const Tex3& SR, const
   return rayleigh_mie;
 }
 // functions.glsl:1285-1330 (50 intervals)
-Spec ComputeMultipleScattering(const Atm& a, const Tex2& T, const Tex3& J, double r,
+ORACLE_HD Spec ComputeMultipleScattering(const Atm& a, const Tex2& T, const Tex3& J, double r,
                                double mu, double mu_s, double nu,
                                bool ray_r_mu_intersects_ground) {
   const int SAMPLE_COUNT = 50;
@@ -591,7 +614,7 @@ Spec ComputeMultipleScattering(const Atm& a, const Tex2& T, const Tex3& J, doubl
   Spec rayleigh_mie_sum;
   for (int i = 0; i <= SAMPLE_COUNT; ++i) {
     double d_i = double(i) * dx;
-    double r_i = ClampRadius(a, std::sqrt(d_i * d_i + 2.0 * r * mu * d_i + r * r));
+    double r_i = ClampRadius(a, om::sqrt(d_i * d_i + 2.0 * r * mu * d_i + r * r));
     double mu_i = ClampCosine((r * mu + d_i) / r_i);
     double mu_s_i = ClampCosine((r * mu_s + d_i * nu) / r_i);
     Spec rayleigh_mie_i =
@@ -603,7 +626,7 @@ Spec ComputeMultipleScattering(const Atm& a, const Tex2& T, const Tex3& J, doubl
   return rayleigh_mie_sum;
 }
 // functions.glsl:1443-1461
-Spec ComputeDirectIrradiance(const Atm& a, const Tex2& T, double r, double mu_s) {
+ORACLE_HD Spec ComputeDirectIrradiance(const Atm& a, const Tex2& T, double r, double mu_s) {
   double alpha_s = a.sun_angular_radius;
   double average_cosine_factor =
       mu_s < -alpha_s ? 0.0
@@ -613,21 +636,21 @@ Spec ComputeDirectIrradiance(const Atm& a, const Tex2& T, double r, double mu_s)
          average_cosine_factor;
 }
 // functions.glsl:1477-1511 (16 x 64 midpoint quadrature over the hemisphere)
-Spec ComputeIndirectIrradiance(const Atm& a, const Tex3& SR, const Tex3& SM,
+ORACLE_HD Spec ComputeIndirectIrradiance(const Atm& a, const Tex3& SR, const Tex3& SM,
                                const Tex3& SMulti, double r, double mu_s,
                                int scattering_order) {
   const int SAMPLE_COUNT = 32;
   const double dphi = kPi / double(SAMPLE_COUNT);
   const double dtheta = kPi / double(SAMPLE_COUNT);
   Spec result;
-  V3 omega_s{std::sqrt(1.0 - mu_s * mu_s), 0.0, mu_s};
+  V3 omega_s{om::sqrt(1.0 - mu_s * mu_s), 0.0, mu_s};
   for (int j = 0; j < SAMPLE_COUNT / 2; ++j) {
     double theta = (double(j) + 0.5) * dtheta;
     for (int i = 0; i < 2 * SAMPLE_COUNT; ++i) {
       double phi = (double(i) + 0.5) * dphi;
-      V3 omega{std::cos(phi) * std::sin(theta), std::sin(phi) * std::sin(theta),
-               std::cos(theta)};
-      double domega = dtheta * dphi * std::sin(theta);
+      V3 omega{om::cos(phi) * om::sin(theta), om::sin(phi) * om::sin(theta),
+               om::cos(theta)};
+      double domega = dtheta * dphi * om::sin(theta);
       double nu = dot(omega, omega_s);
       result += GetScattering(a, SR, SM, SMulti, r, omega.z, mu_s, nu, false,
                               scattering_order) *
@@ -641,13 +664,13 @@ Spec ComputeIndirectIrradiance(const Atm& a, const Tex3& SR, const Tex3& SM,
 // Rendering functions (functions.glsl:1633-1896).
 // ---------------------------------------------------------------------------
 // functions.glsl:1633-1645
-Spec GetExtrapolatedSingleMieScattering(const Atm& a, const Spec& rgb, double alpha) {
+ORACLE_HD Spec GetExtrapolatedSingleMieScattering(const Atm& a, const Spec& rgb, double alpha) {
   if (rgb[0] <= 0.0) return Spec(0.0);
   return rgb * alpha / rgb[0] * (a.rayleigh_scattering[0] / a.mie_scattering[0]) *
          (a.mie_scattering / a.rayleigh_scattering);
 }
 // functions.glsl:1658-1689; S/M are RGBA, combined selects alpha = Mie.r.
-Spec GetCombinedScattering(const Atm& a, const Tex3& S, const double* Sraw, const Tex3& M,
+ORACLE_HD Spec GetCombinedScattering(const Atm& a, const Tex3& S, const double* Sraw, const Tex3& M,
                            bool combined, double r, double mu, double mu_s, double nu,
                            bool ground, Spec* single_mie) {
   double uvw0[3], uvw1[3], lerp;
@@ -675,13 +698,13 @@ Spec GetCombinedScattering(const Atm& a, const Tex3& S, const double* Sraw, cons
   return scattering;
 }
 // functions.glsl:1705-1769
-Spec GetSkyRadiance(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M, bool combined,
+ORACLE_HD Spec GetSkyRadiance(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M, bool combined,
                     V3 camera, const V3& view_ray, double shadow_length,
                     const V3& sun_direction, Spec* transmittance) {
   double r = length(camera);
   double rmu = dot(camera, view_ray);
   double distance_to_top_atmosphere_boundary =
-      -rmu - std::sqrt(rmu * rmu - r * r + a.top_radius * a.top_radius);
+      -rmu - om::sqrt(rmu * rmu - r * r + a.top_radius * a.top_radius);
   if (distance_to_top_atmosphere_boundary > 0.0) {
     camera = camera + view_ray * distance_to_top_atmosphere_boundary;
     r = a.top_radius;
@@ -703,7 +726,7 @@ Spec GetSkyRadiance(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M, b
                                        ray_r_mu_intersects_ground, &single_mie_scattering);
   } else {
     double d = shadow_length;
-    double r_p = ClampRadius(a, std::sqrt(d * d + 2.0 * r * mu * d + r * r));
+    double r_p = ClampRadius(a, om::sqrt(d * d + 2.0 * r * mu * d + r * r));
     double mu_p = (r * mu + d) / r_p;
     double mu_s_p = (r * mu_s + d * nu) / r_p;
     scattering = GetCombinedScattering(a, S, S.p, M, combined, r_p, mu_p, mu_s_p, nu,
@@ -717,14 +740,14 @@ Spec GetSkyRadiance(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M, b
          single_mie_scattering * MiePhaseFunction(a.mie_phase_function_g, nu);
 }
 // functions.glsl:1787-1863
-Spec GetSkyRadianceToPoint(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M,
+ORACLE_HD Spec GetSkyRadianceToPoint(const Atm& a, const Tex2& T, const Tex3& S, const Tex3& M,
                            bool combined, V3 camera, const V3& point, double shadow_length,
                            const V3& sun_direction, Spec* transmittance) {
   V3 view_ray = normalize(point - camera);
   double r = length(camera);
   double rmu = dot(camera, view_ray);
   double distance_to_top_atmosphere_boundary =
-      -rmu - std::sqrt(rmu * rmu - r * r + a.top_radius * a.top_radius);
+      -rmu - om::sqrt(rmu * rmu - r * r + a.top_radius * a.top_radius);
   if (distance_to_top_atmosphere_boundary > 0.0) {
     camera = camera + view_ray * distance_to_top_atmosphere_boundary;
     r = a.top_radius;
@@ -739,8 +762,8 @@ Spec GetSkyRadianceToPoint(const Atm& a, const Tex2& T, const Tex3& S, const Tex
   Spec single_mie_scattering;
   Spec scattering = GetCombinedScattering(a, S, S.p, M, combined, r, mu, mu_s, nu,
                                           ray_r_mu_intersects_ground, &single_mie_scattering);
-  d = std::max(d - shadow_length, 0.0);
-  double r_p = ClampRadius(a, std::sqrt(d * d + 2.0 * r * mu * d + r * r));
+  d = om::max(d - shadow_length, 0.0);
+  double r_p = ClampRadius(a, om::sqrt(d * d + 2.0 * r * mu * d + r * r));
   double mu_p = (r * mu + d) / r_p;
   double mu_s_p = (r * mu_s + d * nu) / r_p;
   Spec single_mie_scattering_p;
@@ -767,13 +790,13 @@ Spec GetSkyRadianceToPoint(const Atm& a, const Tex2& T, const Tex3& S, const Tex
          single_mie_scattering * MiePhaseFunction(a.mie_phase_function_g, nu);
 }
 // functions.glsl:1878-1896
-Spec GetSunAndSkyIrradiance(const Atm& a, const Tex2& T, const Tex2& I, const V3& point,
+ORACLE_HD Spec GetSunAndSkyIrradiance(const Atm& a, const Tex2& T, const Tex2& I, const V3& point,
                             const V3& normal, const V3& sun_direction, Spec* sky_irradiance) {
   double r = length(point);
   double mu_s = dot(point, sun_direction) / r;
   *sky_irradiance = GetIrradiance(a, I, r, mu_s) * ((1.0 + dot(normal, point) / r) * 0.5);
   return a.solar_irradiance * GetTransmittanceToSun(a, T, r, mu_s) *
-         std::max(dot(normal, sun_direction), 0.0);
+         om::max(dot(normal, sun_direction), 0.0);
 }
 
 // ---------------------------------------------------------------------------
@@ -802,18 +825,18 @@ void ParallelFor(long long n, int threads, F&& fn) {
   for (auto& th : pool) th.join();
 }
 
-inline void Store(double* p, const Spec& s, double alpha) {
+ORACLE_HD inline void Store(double* p, const Spec& s, double alpha) {
   p[0] = s[0];
   p[1] = s[1];
   p[2] = s[2];
   p[3] = alpha;
 }
-inline Spec MatVec(const double m[9], const Spec& v) {
+ORACLE_HD inline Spec MatVec(const double m[9], const Spec& v) {
   return Spec(m[0] * v[0] + m[1] * v[1] + m[2] * v[2], m[3] * v[0] + m[4] * v[1] + m[5] * v[2],
               m[6] * v[0] + m[7] * v[1] + m[8] * v[2]);
 }
 
-void ScatteringTexelCoord(const Atm& a, long long idx, double* fx, double* fy, double* fz) {
+ORACLE_HD void ScatteringTexelCoord(const Atm& a, long long idx, double* fx, double* fy, double* fz) {
   int W = a.S_NU * a.S_MU_S;
   *fx = double(idx % W) + 0.5;
   *fy = double((idx / W) % a.S_MU) + 0.5;
@@ -826,7 +849,7 @@ struct Buffers {
 };
 
 // Evaluates one texel of a pass (the *Texture functions of functions.glsl).
-void EvalTexel(int kind, const Atm& a, const Tex2& T, const Tex3& SR, const Tex3& SM,
+ORACLE_HD void EvalTexel(int kind, const Atm& a, const Tex2& T, const Tex3& SR, const Tex3& SM,
                const Tex3& SMulti, const Tex2& I, const Tex3& J, int order, long long idx,
                double* out, double* out2) {
   switch (kind) {

@@ -20,6 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libatmo_oracle.so")
+ORACLE_GPU_SO = os.path.join(HERE, "_build", "libatmo_oracle_gpu.so")
 REF_SO = os.path.join(HERE, "_ref", "libatmo_ref.so")
 
 
@@ -165,6 +166,16 @@ def build(quiet=True):
             or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src)):
         subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC",
                                "-shared", "-pthread", src, "-o", ORACLE_SO])
+    gpu_src = os.path.join(HERE, "atmo_oracle_gpu.cu")
+    stale = lambda so: (not os.path.exists(so) or  # noqa: E731
+                        os.path.getmtime(so) < max(os.path.getmtime(src),
+                                                   os.path.getmtime(gpu_src)))
+    if stale(ORACLE_GPU_SO):
+        # The FP64 GPU oracle: the same evaluators as device code, no FMA
+        # contraction (as the CPU build).
+        subprocess.check_call(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2",
+                               "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                               gpu_src, "-o", ORACLE_GPU_SO])
     ref_src = os.environ.get("ATMO_REFERENCE_DIR", "/root/reference")
     if os.path.isdir(os.path.join(ref_src, "atmosphere")):
         subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"),
@@ -239,6 +250,41 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+_gpu = None
+
+
+def gpu_lib():
+    """The FP64 GPU oracle (atmo_oracle_gpu.cu): the CPU oracle's evaluators
+    as device code, for LUT shapes too large for the CPU."""
+    global _gpu
+    if _gpu is None:
+        if not os.path.exists(ORACLE_GPU_SO):
+            build()
+        L = C.CDLL(ORACLE_GPU_SO)
+        L.oracle_gpu_precompute.restype = C.c_int
+        L.oracle_gpu_precompute.argtypes = [P(Atmosphere), P(Shape), C.c_uint, dp, C.c_int,
+                                            C.c_int, dp, dp, dp, dp]
+        _gpu = L
+    return _gpu
+
+
+def gpu_precompute(atm: Atmosphere, shp, orders=4, lum=None, blend=False, combined=True,
+                   out: Luts | None = None) -> Luts:
+    """precompute() on the GPU in FP64 (needs a CUDA device)."""
+    if not isinstance(shp, Shape):
+        shp = shape(*shp)
+    out = out or Luts(shp)
+    lum = np.ascontiguousarray(IDENTITY if lum is None else np.asarray(lum, np.float64).reshape(9))
+    rc = gpu_lib().oracle_gpu_precompute(C.byref(atm), C.byref(shp), orders, _arr(lum),
+                                         int(blend), int(combined), _arr(out.transmittance),
+                                         _arr(out.scattering),
+                                         _arr(None if combined else out.single_mie),
+                                         _arr(out.irradiance))
+    if rc != 0:
+        raise RuntimeError("GPU oracle precompute failed")
+    return out
 
 
 def ref_lib():

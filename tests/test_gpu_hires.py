@@ -90,3 +90,16 @@ def test_hires_eight_orders_properties(atmo, oracle, torch):
     assert (I1 >= I7).all()
     # The eighth order still adds light somewhere.
     assert (S1[..., :3] > S7[..., :3]).any()
+
+
+def test_hires_eight_orders_vs_gpu_oracle(atmo, oracle, torch):
+    """Every texel of the high-resolution LUTs (8 orders) against the FP64
+    GPU oracle (the CPU oracle's evaluators as device code, pinned to the CPU
+    oracle by tests/test_gpu_oracle.py)."""
+    from parity import TOL_IRRADIANCE
+    atm = hires_earth(oracle)
+    T, S, I = run(atmo, torch, atm, 8)
+    ref = oracle.gpu_precompute(atm, HIRES, 8, combined=True)
+    check("hires transmittance", T.cpu().numpy(), ref.transmittance, TOL_TRANSMITTANCE)
+    check("hires scattering", S.cpu().numpy(), ref.scattering, TOL_SCATTERING, channels=4)
+    check("hires irradiance", I.cpu().numpy(), ref.irradiance, TOL_IRRADIANCE)

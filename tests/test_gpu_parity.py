@@ -246,10 +246,12 @@ def test_model_half_precision(atmo, oracle):
     np.testing.assert_array_equal(m16.transmittance(), m32.transmittance())
 
 
-def oracle_luminance_model(oracle, m, orders, shape):
+def oracle_luminance_model(oracle, m, orders, shape, precompute=None):
     """atmosphere/model.cc:914-963 with the oracle: 3-wavelength groups, the
     CIE luminance_from_radiance matrices, blending, then the transmittance at
-    680/550/440 nm."""
+    680/550/440 nm (precompute: oracle.precompute, or oracle.gpu_precompute
+    for shapes too large for the CPU)."""
+    precompute = precompute or oracle.precompute
     n = (m.num_precomputed_wavelengths + 2) // 3
     dl = (830.0 - 360.0) / (3 * n)
     luts = None
@@ -264,10 +266,10 @@ def oracle_luminance_model(oracle, m, orders, shape):
                 lum[row * 3 + col] = np.float32(
                     (xyz[row * 3] * x + xyz[row * 3 + 1] * y + xyz[row * 3 + 2] * z) * dl)
         atm = oracle.Atmosphere.from_buffer_copy(bytes(m.atmosphere_at(lam)))
-        luts = oracle.precompute(atm, shape, orders, lum=lum, blend=i > 0,
-                                 combined=m.combine_scattering_textures, out=luts)
+        luts = precompute(atm, shape, orders, lum=lum, blend=i > 0,
+                          combined=m.combine_scattering_textures, out=luts)
     atm = oracle.Atmosphere.from_buffer_copy(bytes(m.atmosphere_at()))
-    t = oracle.precompute(atm, shape, 1, combined=True)
+    t = precompute(atm, shape, 1, combined=True)
     luts.transmittance[...] = t.transmittance
     return luts
 
