@@ -58,14 +58,15 @@ PERTURBATION = 1e-13
 ROBUST_THRESHOLD = 1e-5
 
 
-def robust_masks(O, atm, shape, orders, combined=True, base=None):
+def robust_masks(O, atm, shape, orders, combined=True, base=None, precompute=None):
     """Masks of the texels to compare: True where the oracle's value is not
-    dominated by FP64 rounding."""
+    dominated by FP64 rounding (precompute: O.precompute or O.gpu_precompute)."""
+    precompute = precompute or O.precompute
     b = O.Atmosphere.from_buffer_copy(bytes(atm))
     b.bottom_radius *= 1.0 + PERTURBATION
     b.top_radius *= 1.0 + PERTURBATION
-    base = base or O.precompute(atm, shape, orders, combined=combined)
-    pert = O.precompute(b, shape, orders, combined=combined)
+    base = base or precompute(atm, shape, orders, combined=combined)
+    pert = precompute(b, shape, orders, combined=combined)
     masks = {}
     for k in ("transmittance", "scattering", "single_mie", "irradiance"):
         ch = 4 if (k == "scattering" and combined) else 3

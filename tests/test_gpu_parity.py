@@ -117,6 +117,37 @@ def test_odd_sizes_vs_oracle(atmo, oracle, torch, path):
 
 
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
+@pytest.mark.parametrize("combined", [True, False], ids=["combined", "separate"])
+def test_default_shape_every_texel_vs_gpu_oracle(atmo, oracle, torch, path, combined):
+    """Config 0 (Earth, the reference's default LUT sizes, 4 orders): every
+    texel against the FP64 GPU oracle (the golden test above samples texels
+    of the reference build's own LUTs)."""
+    atm = oracle.earth_atmosphere()
+    shape = atmo.DEFAULT_SHAPE
+    ref = oracle.gpu_precompute(atm, shape, 4, combined=combined)
+    compare(ref, gpu_precompute(atmo, torch, atm, shape, 4, combined, path), combined)
+
+
+def test_double_r_random_atmospheres_vs_gpu_oracle(atmo, oracle, torch):
+    """Random planets of the batched configuration at its largest size
+    (double-R: 256 x 64 / R 64 x MU 128 x MU_S 32 x NU 8 / 64 x 16), 2 and 6
+    orders, every texel where the FP64 values are not rounding-dominated
+    (masks from the FP64 GPU oracle)."""
+    from precomputed_atmospheric_scattering_gb300.workloads import DOUBLE_R
+    rng = np.random.default_rng(77)
+    for orders in (2, 6):
+        atm = random_atmosphere(oracle, rng)
+        ref, masks = robust_masks(oracle, atm, DOUBLE_R, orders, False,
+                                  precompute=oracle.gpu_precompute)
+        T, S, M, I = gpu_precompute(atmo, torch, atm, DOUBLE_R, orders, False, 0)
+        check_masked("transmittance", T, ref.transmittance, TOL_TRANSMITTANCE,
+                     masks["transmittance"])
+        check_masked("scattering", S, ref.scattering, TOL_SCATTERING, masks["scattering"])
+        check_masked("single_mie", M, ref.single_mie, TOL_SCATTERING, masks["single_mie"])
+        check_masked("irradiance", I, ref.irradiance, TOL_IRRADIANCE, masks["irradiance"])
+
+
+@pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
 def test_medium_shape_random_atmospheres_vs_oracle(atmo, oracle, torch, path):
     """Non-Earth planets: seeded draws over the batched-rebuild ranges, compared
     on the texels where the FP64 reference is not rounding-dominated."""
