@@ -17,6 +17,10 @@
 // point is at r = Rb, on row 0's centre), also staged in shared memory.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+
 #include "atmo_kernels.h"
 #include "atmo_passes.cuh"
 
@@ -141,7 +145,10 @@ struct MergeRow {
   uint32_t adj;       // address adjustment of the row's table
   uint32_t jstride;   // J x kNodeBytes; 0 when the row is not merged
 };
-constexpr int kMergeBudgetCap = 24 * 1024;
+// Above order 2 a block is limited to 2 per SM by its registers, so its
+// shared memory may grow to ~99 KB (opted in above the default 48 KB) at no
+// cost in occupancy.
+constexpr int kDensityMaxSmem = 99 * 1024;
 
 // Shared memory of one block, bytes, without the merged tables: [16][NU + 1]
 // entries (the previous order interpolated in mu at the slab's r and mu_s;
@@ -156,16 +163,41 @@ __host__ __device__ inline int DensityBaseSmem(const Shape& s, int order) {
          (species * nodes + s.iw) * 16 +
          (order == 2 ? 0 : kDensityThetaSamples * (int)(sizeof(MergeRow) + sizeof(int4)) + 16);
 }
-// The merged tables' budget above order 2: what keeps the block within 48 KB,
-// at most kMergeBudgetCap.
-__host__ __device__ inline int DensityMergeBytes(const Shape& s) {
-  int b = 48 * 1024 - DensityBaseSmem(s, 3);
-  b = b < 0 ? 0 : (b > kMergeBudgetCap ? kMergeBudgetCap : b);
-  return b / kNodeBytes * kNodeBytes;
+// The merged tables a block of the instance may need above order 2, bytes:
+// the largest r-slice's sum over its ground rows of (NU + 1) J entries, with
+// J bounded from the ray's distance to the ground (the FP64 geometry of the
+// set-up tables at the slice's r and cos(theta_l), plus a margin for the
+// rounding of both ends).  Only a budget: rows that do not fit it keep the
+// separate sky and ground lookups.
+int DensityMergeNeed(const Shape& s, const Consts& c) {
+  const double Rb = c.dRb, H = c.dH, pi = 3.14159265358979323846;
+  const double k1 = double(s.snu - 1) / (2.0 * s.snu), kg = double(s.iw - 1) / (2.0 * s.iw);
+  int worst = 0;
+  for (int k = 0; k < s.sr; ++k) {
+    const double rho = H * k / double(s.sr > 1 ? s.sr - 1 : 1);
+    const double r = std::sqrt(rho * rho + Rb * Rb);
+    int entries = 0;
+    for (int l = 0; l < kDensityThetaSamples; ++l) {
+      const double mu = std::cos((l + 0.5) * pi / kDensityThetaSamples);
+      const double disc = r * r * (mu * mu - 1.0) + Rb * Rb;
+      if (mu >= 0.0 || disc < 0.0) continue;
+      const double gs = kg * (-r * mu - std::sqrt(disc)) / (Rb * k1);
+      const int J = std::min((int)std::floor(gs * s.iw) + 3, s.iw + 1);
+      entries += (s.snu + 1) * J;
+    }
+    worst = std::max(worst, entries);
+  }
+  return worst * kNodeBytes;
 }
-int DensityFastSmem(const Shape& s, int order) {
-  return DensityBaseSmem(s, order) + (order == 2 ? 0 : DensityMergeBytes(s));
+int DensityFastSmem(const Shape& s, const Consts& c, int order) {
+  const int base = DensityBaseSmem(s, order);
+  if (order == 2) return base;
+  const int room = kDensityMaxSmem - base;
+  const int merge = std::min(DensityMergeNeed(s, c), room > 0 ? room : 0);
+  return base + merge / kNodeBytes * kNodeBytes;
 }
+
+
 // Shapes whose order-2 tables (the larger) fit the default 48 KB per block;
 // the others take the plain density kernel.
 bool DensityFastFits(const Shape& s) { return DensityBaseSmem(s, 2) <= 48 * 1024; }
@@ -289,7 +321,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
 
 template <bool kOrder2>
 __global__ void __launch_bounds__(kDensityFastThreads)
-k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
+k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) {
   extern __shared__ float4 smem[];
   constexpr int kSpecies = kOrder2 ? 2 : 1;
   constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
@@ -366,7 +398,8 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   __syncthreads();
   if (!kOrder2 && threadIdx.x == 0) {
     // Table offsets, rows in theta order while they fit the budget.
-    const int budget = DensityMergeBytes(s) / kNodeBytes;
+    // The budget: the launch's shared memory beyond this instance's tables.
+    const int budget = max(smem_bytes - DensityBaseSmem(s, 3), 0) / kNodeBytes;
     const uint32_t xbase = (uint32_t)__cvta_generic_to_shared(X);
     int off = 0;
     for (int l = 0; l < kDensityThetaSamples; ++l) {
@@ -497,14 +530,34 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl) {
   }
 }
 
+// Lets k_density_fast<false> take kDensityMaxSmem (once per device; every
+// later call is a lock-free check).  Called before a CUDA graph capture and
+// by the launcher.
+cudaError_t PrepareDensityFast() {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(k_density_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kDensityMaxSmem);
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
                               int smem_bytes, cudaStream_t st) {
   // smem_bytes: the largest DensityFastSmem of the work list's instances.
   const size_t bytes = (size_t)smem_bytes;
   if (order == 2) {
-    k_density_fast<true><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl);
+    k_density_fast<true><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, smem_bytes);
   } else {
-    k_density_fast<false><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl);
+    if (smem_bytes > 48 * 1024) {
+      const cudaError_t e = PrepareDensityFast();
+      if (e != cudaSuccess) return e;
+    }
+    k_density_fast<false><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, smem_bytes);
   }
   return cudaGetLastError();
 }

@@ -25,7 +25,8 @@ cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
                                 cudaStream_t st);
 // Fast path (atmo_fast.cu).
 int DensityFastTiles(const Shape& s);
-int DensityFastSmem(const Shape& s, int order);
+int DensityFastSmem(const Shape& s, const Consts& c, int order);
+cudaError_t PrepareDensityFast();
 bool DensityFastFits(const Shape& s);
 cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int order,
                               int smem_bytes, cudaStream_t st);

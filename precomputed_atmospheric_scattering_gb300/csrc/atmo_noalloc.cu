@@ -110,6 +110,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     return ATMO_INVALID_ARG;
   }
   const Shape s = ToShape(ls);
+  const Consts consts = MakeConsts(*atmosphere, lum);
 
   // The pass sequence of atmosphere/model.cc:1048-1215 for one instance:
   // each step's work list is {inst = 0; start = 0, tiles}.
@@ -122,7 +123,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
   auto add = [&](Pass p, int order) {
     const atmo_path path = PassPath(p, s, ATMO_PATH_FAST);
     steps.push_back(
-        PlannedStep{p, order, Tiles(p, s, path), SharedBytes(p, s, order, path), path});
+        PlannedStep{p, order, Tiles(p, s, path), SharedBytes(p, s, consts, order, path), path});
   };
   add(Pass::kTables, 0);
   add(Pass::kTransmittance, 0);
@@ -169,7 +170,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
 
   Instance in;
   std::memset(&in, 0, sizeof(in));
-  in.c = MakeConsts(*atmosphere, lum);
+  in.c = consts;
   in.s = s;
   in.T = reinterpret_cast<float4*>(transmittance);
   in.S = reinterpret_cast<float4*>(scattering);

@@ -127,9 +127,9 @@ atmo_path PassPath(Pass pass, const Shape& s, atmo_path path) {
   return path;
 }
 
-int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path) {
+int SharedBytes(Pass pass, const Shape& s, const Consts& c, int order, atmo_path path) {
   if (path != ATMO_PATH_FAST) return 0;
-  if (pass == Pass::kDensity) return DensityFastSmem(s, order);
+  if (pass == Pass::kDensity) return DensityFastSmem(s, c, order);
   if (pass == Pass::kMultiple) return MultipleFastSmem(s);
   if (pass == Pass::kSingle) return SingleFastSmem(s);
   if (pass == Pass::kIndirect) return IndirectSmem(s, order);
@@ -185,7 +185,7 @@ int Program::AddWorkList(const std::vector<int>& members, Pass pass, int order, 
     start.push_back(t);
     t += Tiles(pass, slots[m].s, p);
     if (smem) {
-      int b = SharedBytes(pass, slots[m].s, order, p);
+      int b = SharedBytes(pass, slots[m].s, slots[m].c, order, p);
       *smem = b > *smem ? b : *smem;
     }
   }
@@ -345,6 +345,8 @@ atmo_status Program::Run(cudaStream_t st, bool use_graph) {
       ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
     }
     cudaGraph_t g = nullptr;
+    // Kernel attributes are set before the capture, not inside it.
+    ATMO_CUDA_TRY(PrepareDensityFast());
     ATMO_CUDA_TRY(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
     atmo_status ls = Launch(capture_stream_);
     cudaError_t ce = cudaStreamEndCapture(capture_stream_, &g);

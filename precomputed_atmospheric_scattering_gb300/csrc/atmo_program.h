@@ -104,7 +104,9 @@ atmo_path PassPath(Pass pass, const Shape& s, atmo_path path);
 // Blocks and dynamic shared memory of `pass` for shape s under the variant
 // `path` (as PassPath returns it).
 int Tiles(Pass pass, const Shape& s, atmo_path path);
-int SharedBytes(Pass pass, const Shape& s, int order, atmo_path path);
+// Dynamic shared memory of a pass's launch for one instance (shape and
+// constants: the density pass sizes its merged tables from the radii).
+int SharedBytes(Pass pass, const Shape& s, const Consts& c, int order, atmo_path path);
 // Launches one pass over the instances of `wl` (device pointers); kToHalf is
 // not a pass kernel and returns cudaErrorInvalidValue.
 cudaError_t LaunchPass(Pass pass, int order, int smem, const Instance* insts, WorkList wl,

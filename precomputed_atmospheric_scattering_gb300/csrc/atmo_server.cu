@@ -447,7 +447,8 @@ bool atmo_server::LaunchRound() {
       h[off + i] = g.members[i]->index;
       h[off + n + i] = t;
       t += Tiles(g.pass, g.members[i]->s, g.path);
-      smem = std::max(smem, SharedBytes(g.pass, g.members[i]->s, g.order, g.path));
+      smem = std::max(smem, SharedBytes(g.pass, g.members[i]->s, h_inst[g.members[i]->index].c,
+                                        g.order, g.path));
     }
     h[off + 2 * n] = t;
     WorkList wl;
