@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <type_traits>
 
 #include "atmo_kernels.h"
 #include "atmo_passes.cuh"
@@ -47,12 +48,33 @@ int DensityFastTiles(const Shape& s) { return s.sr * s.smus; }
 constexpr float kRoundMagic = 12582912.0f;
 constexpr uint32_t kRoundMagicBits = 0x4B400000u;
 
-// One entry: a.xyz, b.x | b.y, b.z, -, -.
+// One entry: a.xyz, b.x | b.y, b.z, -, - at order 2; above order 2 (packed)
+// a.xy, b.xy | a.z, b.z, -, -, the x, y channels as aligned register pairs
+// for the packed FP32x2 FMA.
 constexpr int kNodeBytes = 32;
 // One order-2 entry, the Rayleigh and the Mie lines in 48 bytes:
 // aR.xyz, bR.x | bR.yz, aM.xy | aM.z, bM.xyz.  The 48-byte stride also puts
 // the 8 entries of a 16-bank span on disjoint banks.
 constexpr int kPairBytes = 48;
+
+// Three channels as a register pair (x, y) and a scalar (z) for the packed
+// FP32x2 instructions (per component the same IEEE operations as fmaf and
+// fadd, so the sums are bit-identical to the scalar ones).  Above order 2 the
+// density kernel is bound by instruction issue, and the packed FMAs and adds
+// of its lookups and sums save ~3% of its time.  At order 2 they do not pay:
+// its code stays scalar.
+struct P3 {
+  float2 xy;
+  float z;
+};
+__device__ __forceinline__ float2 Dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ P3 ToP3(F3 a) { return P3{make_float2(a.x, a.y), a.z}; }
+__device__ __forceinline__ F3 ToF3(P3 a) { return F3{a.xy.x, a.xy.y, a.z}; }
+__device__ __forceinline__ F3 ToF3(F3 a) { return a; }
+__device__ __forceinline__ P3 Fma(P3 a, P3 b, P3 c) {
+  return P3{__ffma2_rn(a.xy, b.xy, c.xy), fmaf(a.z, b.z, c.z)};
+}
+__device__ __forceinline__ P3 Add(P3 a, P3 b) { return P3{__fadd2_rn(a.xy, b.xy), a.z + b.z}; }
 
 // a b + c clamped to [0, 1], NaN to 0 (one FMA with the .sat modifier).
 __device__ __forceinline__ float FmaSat(float a, float b, float c) {
@@ -89,22 +111,29 @@ __device__ __forceinline__ void EntryLine(const float4* v, int e, int N, F3* a, 
   *a = fma3(d, c, F3{p.x, p.y, p.z});
   *b = d * float(N);
 }
+template <bool kPacked>
 __device__ __forceinline__ void StoreLine(float4* entry, F3 a, F3 b) {
-  entry[0] = make_float4(a.x, a.y, a.z, b.x);
-  entry[1] = make_float4(b.y, b.z, 0.0f, 0.0f);
+  if (kPacked) {
+    entry[0] = make_float4(a.x, a.y, b.x, b.y);
+    entry[1] = make_float4(a.z, b.z, 0.0f, 0.0f);
+  } else {
+    entry[0] = make_float4(a.x, a.y, a.z, b.x);
+    entry[1] = make_float4(b.y, b.z, 0.0f, 0.0f);
+  }
 }
 // Entry e (0 <= e <= N) of a row of N node values v[0..N-1].
+template <bool kPacked>
 __device__ __forceinline__ void StoreEntry(float4* entry, const float4* v, int e, int N) {
   F3 a, b;
   EntryLine(v, e, N, &a, &b);
-  StoreLine(entry, a, b);
+  StoreLine<kPacked>(entry, a, b);
 }
 // Entry e of a row of N Rayleigh values r[] and Mie values m[] (order 2).
 __device__ __forceinline__ void StorePairEntry(float4* entry, const float4* r, const float4* m,
                                                int e, int N) {
   float4 a[2], b[2];
-  StoreEntry(a, r, e, N);
-  StoreEntry(b, m, e, N);
+  StoreEntry<false>(a, r, e, N);
+  StoreEntry<false>(b, m, e, N);
   entry[0] = a[0];
   entry[1] = make_float4(a[1].x, a[1].y, b[0].x, b[0].y);
   entry[2] = make_float4(b[0].z, b[0].w, b[1].x, b[1].y);
@@ -118,6 +147,16 @@ __device__ __forceinline__ F3 EvalNodes(float s, float t, uint32_t row_adj) {
   const float4 p = LoadShared4<kOffset>(a);
   const float2 q = LoadShared2<kOffset + 16>(a);
   return F3{fmaf(s, p.w, p.x), fmaf(s, q.x, p.y), fmaf(s, q.y, p.z)};
+}
+// The line of the packed entry at shared address a, at s.
+__device__ __forceinline__ P3 PackedLine(float s, uint32_t a) {
+  const float4 p = LoadShared4<0>(a);
+  const float2 q = LoadShared2<16>(a);
+  return P3{__ffma2_rn(Dup(s), make_float2(p.z, p.w), make_float2(p.x, p.y)), fmaf(s, q.y, q.x)};
+}
+// EvalNodes for a packed table of kNodeBytes entries.
+__device__ __forceinline__ P3 EvalNodesPacked(float s, float t, uint32_t row_adj) {
+  return PackedLine(s, (uint32_t)__float_as_int(t) * (uint32_t)kNodeBytes + row_adj);
 }
 // Both lines of an order-2 entry (kPairBytes apart).
 __device__ __forceinline__ void EvalPair(float s, float t, uint32_t row_adj, F3* ray, F3* mie) {
@@ -216,8 +255,9 @@ __host__ __device__ constexpr int DensityTexelsPerTask() { return 4; }
 template <bool kOrder2>
 struct DensityTask {
   static constexpr int kN = DensityTexelsPerTask<kOrder2>();
+  using V = std::conditional_t<kOrder2, F3, P3>;   // packed above order 2
   float sx[kN], sy[kN];   // the sun's x, y
-  F3 sum[kN];             // order 2: sums of L P_R(nu2) dw; else L (a_R P_R + a_M P_M) dw
+  V sum[kN];              // order 2: sums of L P_R(nu2) dw; else L (a_R P_R + a_M P_M) dw
   F3 sum_m[kOrder2 ? kN : 1];   // order 2: sums of L P_M(nu2) dw
 };
 
@@ -240,7 +280,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
                                                 uint32_t ir_adj, uint32_t jstride = 0,
                                                 uint32_t madj = 0) {
   static_assert(!kMerged || (kGround && !kOrder2), "merged tables: ground rows above order 2");
-  constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
+  using V = typename DensityTask<kOrder2>::V;
   constexpr int kDensityTexelsPerTask = DensityTexelsPerTask<kOrder2>();
   const float m2g = c.m2g, g2p1 = c.g2p1;
   // phi and 2 pi - phi share cos(phi), hence nu2 and the phase functions of
@@ -257,7 +297,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
     const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
     // Order 2: war.x = wam.x = dw.
     const float pr = kOrder2 ? q2 * war.x : 0.0f, pm = kOrder2 ? pr * (rs * rs * rs) : 0.0f;
-    const F3 w = kOrder2 ? f3(0.0f) : fma3(wam, q2 * (rs * rs * rs), war * q2);
+    const P3 w = ToP3(kOrder2 ? f3(0.0f) : fma3(wam, q2 * (rs * rs * rs), war * q2));
     const float hc = cs.x * hs, hn = cs.y * hs;
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
@@ -265,31 +305,25 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
       const float bu = fmaf(task.sx[q], hc, A);
       // Ls is seeded with the first side's radiance (an explicit 0 + x
       // would cost an add per channel: IEEE keeps it).
-      F3 Ls;
+      V Ls;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         const float u = FmaSat(side == 0 ? hn : -hn, task.sy[q], bu);
         const float t = fmaf(u, fnu, kRoundMagic);
-        if (kMerged) {
+        if constexpr (kMerged) {
           // Entry (i, j) of the merged table: one line in s for sky + ground.
           const float x = FmaSat(u, g_scale, g_off);
           const uint32_t a = (uint32_t)__float_as_int(t) * jstride +
                              (uint32_t)__float_as_int(fmaf(x, fiw, kRoundMagic)) *
                                  (uint32_t)kNodeBytes +
                              madj;
-          const float4 p = LoadShared4<0>(a);
-          const float2 r = LoadShared2<16>(a);
-          const F3 L{fmaf(u, p.w, p.x), fmaf(u, r.x, p.y), fmaf(u, r.y, p.z)};
-          Ls = side == 0 ? L : Ls + L;
+          const P3 L = PackedLine(u, a);
+          Ls = side == 0 ? L : Add(Ls, L);
           continue;
         }
-        F3 L, M;
-        if (kOrder2) {
+        if constexpr (kOrder2) {
+          F3 L, M;
           EvalPair(u, t, row_adj, &L, &M);
-        } else {
-          L = EvalNodes<kStride, 0>(u, t, row_adj);
-        }
-        if (kOrder2) {
           // Single scattering with its phase functions at nu1 (:998-1004):
           // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
           // with the constant factors staged into the tables.
@@ -299,21 +333,27 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
           const float q1 = fmaf(nu1, nu1, 1.0f);
           Ls = side == 0 ? L1 * q1 : fma3(L1, q1, Ls);
         } else {
-          Ls = side == 0 ? L : Ls + L;
+          const P3 L = EvalNodesPacked(u, t, row_adj);
+          Ls = side == 0 ? L : Add(Ls, L);
         }
         if (kGround) {
           // Ground bounce: the ground point is at radius Rb, so the cosine
           // of its normal with the sun is (r mu_s + dist nu1) / Rb; the
           // irradiance lookup at r = Rb reads row 0 of the LUT.
           const float x = FmaSat(u, g_scale, g_off);
-          Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, fmaf(x, fiw, kRoundMagic), ir_adj), Ls);
+          const float xt = fmaf(x, fiw, kRoundMagic);
+          if constexpr (kOrder2) {
+            Ls = fma3(tg, EvalNodes<kNodeBytes, 0>(x, xt, ir_adj), Ls);
+          } else {
+            Ls = Fma(ToP3(tg), EvalNodesPacked(x, xt, ir_adj), Ls);
+          }
         }
       }
-      if (kOrder2) {
+      if constexpr (kOrder2) {
         task.sum[q] = fma3(Ls, pr, task.sum[q]);
         task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
       } else {
-        task.sum[q] = fma3(Ls, w, task.sum[q]);
+        task.sum[q] = Fma(Ls, w, task.sum[q]);
       }
     }
   }
@@ -430,11 +470,11 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       if (kOrder2) {
         StorePairEntry(E + e * (kPairBytes / 16), V + l * NU, V + nodes + l * NU, i, NU);
       } else {
-        StoreEntry(E + e * (kNodeBytes / 16), V + l * NU, i, NU);
+        StoreEntry<true>(E + e * (kNodeBytes / 16), V + l * NU, i, NU);
       }
     } else if (e < base_entries) {
       const int i = e - sky_entries;
-      StoreEntry(G + i * (kNodeBytes / 16), V + kSpecies * nodes, i, s.iw);
+      StoreEntry<!kOrder2>(G + i * (kNodeBytes / 16), V + kSpecies * nodes, i, s.iw);
     } else if (!kOrder2) {
       // Merged entry (i, j) of row l: sky line + tg (ground line at gs s + go).
       const int m = e - base_entries;
@@ -447,7 +487,7 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       EntryLine(V + nodes, j, s.iw, &ga, &gb);
       const F3 tg = f3(drows[l].t_ground);
       const MergeRow mr = meta[l];
-      StoreLine(X + m * (kNodeBytes / 16), fma3(tg, fma3(gb, mr.go, ga), sa),
+      StoreLine<true>(X + m * (kNodeBytes / 16), fma3(tg, fma3(gb, mr.go, ga), sa),
                 fma3(tg, gb * mr.gs, sb));
     }
   }
@@ -467,7 +507,7 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       const TexelAngles ang = MakeAngles(s, row, cc, min(n0 + q, NU - 1));
       task.sx[q] = ang.sx;
       task.sy[q] = ang.sy;
-      task.sum[q] = f3(0.0f);
+      task.sum[q] = typename DensityTask<kOrder2>::V{};
       task.sum_m[kOrder2 ? q : 0] = f3(0.0f);
     }
     // The scattering coefficients at the texel, with the phase constants
@@ -523,7 +563,8 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
       if (n0 + q < NU) {
-        const F3 J = kOrder2 ? a_r * task.sum[q] + a_m * task.sum_m[q] : task.sum[q];
+        const F3 J =
+            kOrder2 ? a_r * ToF3(task.sum[q]) + a_m * task.sum_m[q] : ToF3(task.sum[q]);
         in.dJ[(k * s.smu + j) * W + (n0 + q) * s.smus + col] = to4(J, 1.0f);
       }
     }
