@@ -19,7 +19,10 @@ Reported (one JSON line on rank 0):
   single_rebuild p50/p99 latency of one Model.Init (fast path) and the plain
                  path's rebuilds/s,
   roofline       the scattering-density kernel against this GPU's FP32 FMA
-                 throughput measured in the same run,
+                 throughput measured in the same run: the reference
+                 algorithm's FLOPs per direction sample (counted in the
+                 oracle, tests/golden/flops_config0.json) over the launch
+                 time, and the FLOPs the kernel executes (ncu),
   parity         per-LUT max / p99 relative error of the benchmarked LUTs at
                  the FP64 reference's committed sampled texels,
   batched_mixed  256 seeded planets of uneven LUT shapes ({half, default,
@@ -54,12 +57,25 @@ METRIC = "Earth LUT rebuilds/s batched vs plain on 1 GB300 @<=1e-3 vs FP64; p99 
 UNIT = "rebuilds/s"
 WORKLOAD = ("Earth atmosphere LUT rebuild, 256x64 / 256x128x32 / 64x16 RGBA FP32, "
             "4 scattering orders, 3 wavelengths, combined textures")
-# FP32 operations per direction sample of the fast scattering-density kernel
-# (FADD + FMUL + 2 x FFMA, counted by ncu's SASS op counters over one launch:
-# profiles/fast_kernels_earth_default_batch2.md): order 2 evaluates single
-# scattering with its phase functions, higher orders one radiance table (one
-# merged sky + ground table on the rows that hit the ground).
+# FP32 operations per direction sample that the fast scattering-density kernel
+# executes (FADD + FMUL + 2 x FFMA, counted by ncu's SASS op counters over one
+# launch: profiles/fast_kernels_earth_default_batch2.md): order 2 evaluates
+# single scattering with its phase functions, higher orders one radiance table
+# (one merged sky + ground table on the rows that hit the ground).
 DENSITY_FLOPS_PER_SAMPLE = {2: 50.9, 3: 20.1}
+# The reference algorithm's operation counts of this workload, frozen from the
+# oracle's counting build (tests/golden/make_flops.py): adds and muls of the
+# shader arithmetic per direction sample of each density launch, and per
+# rebuild.
+FLOPS_CONFIG0 = os.path.join(ROOT, "tests", "golden", "flops_config0.json")
+
+
+def reference_flops():
+    with open(FLOPS_CONFIG0) as f:
+        d = json.load(f)
+    per_sample = {l["order"]: l["flops_per_unit"] for l in d["counts"]["launches"]
+                  if l["pass"] == "scattering_density"}
+    return per_sample, d["counts"]["total"]["flops"]
 # DRAM bytes per density launch and instance, from the same capture
 # (dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance launch / 2).
 DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.25e6}
@@ -333,7 +349,7 @@ def run_gpu(args):
 
     # --- roofline of the scattering-density kernel ---------------------------
     peak = atmo.measure_fp32_peak()
-    roof = roofline_entry(batch, B, peak, stream)
+    roof = roofline_entry(batch, B, peak, stream, value / world)
     del batch, single
     torch.cuda.empty_cache()
 
@@ -397,18 +413,36 @@ def time_plain(atmo, W, torch, stream, args):
     return sorted(out)[1]
 
 
-def roofline_entry(batch, B, peak, stream):
+def roofline_entry(batch, B, peak, stream, rebuilds_per_s):
     passes = batch.time_passes(stream)
     dens = [(o, ms) for name, o, ms in passes if name == "scattering_density"]
     total = sum(ms for _, _, ms in passes)
     # One launch covers B instances x 1,048,576 texels x 512 directions.
     samples = B * 1048576 * 512
-    flops = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
     dens_ms = sum(ms for _, ms in dens)
-    achieved = flops / (dens_ms * 1e-3) / 1e12
+    ref_per_sample, ref_rebuild = reference_flops()
+    algorithmic = sum(ref_per_sample[min(o, 3)] * samples for o, _ in dens)
+    achieved = algorithmic / (dens_ms * 1e-3) / 1e12
+    executed = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
+    executed_rate = executed / (dens_ms * 1e-3) / 1e12
     traffic = sum(DENSITY_DRAM_BYTES_PER_INSTANCE[min(o, 3)] * B for o, _ in dens) / len(dens)
     return {"bound": "fp32", "kernel": "scattering density",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "flops": "the reference algorithm's: adds and muls of ComputeScatteringDensity "
+                     "per direction sample, counted in the oracle (%s); the restructured "
+                     "kernel executes fewer (see executed), so frac exceeds 1"
+                     % os.path.relpath(FLOPS_CONFIG0, ROOT),
+            "algorithmic_flops_per_sample": {str(k): round(v, 2)
+                                             for k, v in sorted(ref_per_sample.items())},
+            "executed": {"flops_per_sample": {str(k): v
+                                              for k, v in DENSITY_FLOPS_PER_SAMPLE.items()},
+                         "achieved": executed_rate, "frac": executed_rate / peak,
+                         "source": "ncu SASS op counters (FADD + FMUL + 2 FFMA) of one launch"},
+            "rebuild": {"algorithmic_flops": ref_rebuild,
+                        "achieved": ref_rebuild * rebuilds_per_s / 1e12,
+                        "frac": ref_rebuild * rebuilds_per_s / 1e12 / peak,
+                        "note": "all passes of one rebuild, reference-algorithm FLOPs x the "
+                                "batched rebuilds/s"},
             "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance "
                               "launch per order (profiles/fast_kernels_earth_default_batch2.md), "
@@ -418,7 +452,6 @@ def roofline_entry(batch, B, peak, stream):
                            "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
             "avg_launch_ms": dens_ms / len(dens), "launches_per_step": len(dens),
             "share_of_step": dens_ms / total,
-            "flops_per_sample": {str(k): v for k, v in DENSITY_FLOPS_PER_SAMPLE.items()},
             "passes_ms": {n + ("" if o == 0 else str(o)): round(ms, 4)
                           for n, o, ms in passes}}
 

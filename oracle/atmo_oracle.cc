@@ -33,7 +33,9 @@ constexpr double kPi = 3.14159265358979323846;
 
 // The math of the texel evaluators, callable from host and (in the FP64 GPU
 // build, atmo_oracle_gpu.cu) device code: the C library functions, and
-// min / max with the std:: semantics.
+// min / max with the std:: semantics.  The FLOP-counting build
+// (atmo_oracle_count.cc) supplies its own, over its counting scalar type.
+#ifndef ORACLE_COUNTING
 namespace om {
 ORACLE_HD inline double sqrt(double x) { return ::sqrt(x); }
 ORACLE_HD inline double exp(double x) { return ::exp(x); }
@@ -47,6 +49,15 @@ ORACLE_HD inline T min(T a, T b) { return b < a ? b : a; }
 template <class T>
 ORACLE_HD inline T max(T a, T b) { return a < b ? b : a; }
 }  // namespace om
+#endif
+
+// Hooks of the FLOP-counting build: the pass a texel evaluation belongs to,
+// and the texture-filtering scope (GL filtering is done by the texture unit in
+// the reference, so its arithmetic is counted apart).  Empty otherwise.
+#ifndef ORACLE_COUNT_PASS
+#define ORACLE_COUNT_PASS(kind)
+#define ORACLE_COUNT_FILTER()
+#endif
 
 // ---------------------------------------------------------------------------
 // Small vector types (the GLSL vec3 / spectrum of atmosphere/definitions.glsl)
@@ -131,6 +142,7 @@ struct Tex3 {
 };
 
 ORACLE_HD Spec texture(const Tex2& t, double u, double v) {
+  ORACLE_COUNT_FILTER();
   double x = u * t.w - 0.5, y = v * t.h - 0.5;
   double fi = om::floor(x), fj = om::floor(y);
   int i = (int)fi, j = (int)fj;
@@ -140,6 +152,7 @@ ORACLE_HD Spec texture(const Tex2& t, double u, double v) {
 }
 
 ORACLE_HD Spec texture(const Tex3& t, double u, double v, double w) {
+  ORACLE_COUNT_FILTER();
   double x = u * t.w - 0.5, y = v * t.h - 0.5, z = w * t.d - 0.5;
   double fi = om::floor(x), fj = om::floor(y), fk = om::floor(z);
   int i = (int)fi, j = (int)fj, k = (int)fk;
@@ -156,6 +169,7 @@ ORACLE_HD Spec texture(const Tex3& t, double u, double v, double w) {
 
 // Texel taps (clamped flat indices and weights) of the 3D lookup above.
 ORACLE_HD void texture_taps(const Tex3& t, double u, double v, double w, int idx[8], double wt[8]) {
+  ORACLE_COUNT_FILTER();
   double x = u * t.w - 0.5, y = v * t.h - 0.5, z = w * t.d - 0.5;
   double fi = om::floor(x), fj = om::floor(y), fk = om::floor(z);
   int i = (int)fi, j = (int)fj, k = (int)fk;
@@ -852,6 +866,7 @@ struct Buffers {
 ORACLE_HD void EvalTexel(int kind, const Atm& a, const Tex2& T, const Tex3& SR, const Tex3& SM,
                const Tex3& SMulti, const Tex2& I, const Tex3& J, int order, long long idx,
                double* out, double* out2) {
+  ORACLE_COUNT_PASS(kind);
   switch (kind) {
     case 0: {  // functions.glsl:454-463
       double fx = double(idx % a.T_W) + 0.5, fy = double(idx / a.T_W) + 0.5;
@@ -914,7 +929,9 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
   auto tick = Clock::now();
   auto lap = [&](int slot) {
     auto now = Clock::now();
-    if (seconds) seconds[slot] += std::chrono::duration<double>(now - tick).count();
+    if (seconds)
+      seconds[slot] +=
+          1e-9 * (double)std::chrono::duration_cast<std::chrono::nanoseconds>(now - tick).count();
     tick = now;
   };
   const long long nT = (long long)a.T_W * a.T_H;
@@ -986,6 +1003,7 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
     });
     dI.swap(newI);
     DI.p = dI.data();
+    ORACLE_COUNT_PASS(4);
     for (long long i = 0; i < nI; ++i) {
       Spec add = MatVec(lum, Spec::From(dI.data() + 4 * i));
       double* p = irradiance + 4 * i;
@@ -1249,7 +1267,7 @@ double oracle_cie_table_value(double wavelength, int column) {
   // atmosphere/model.cc:521-533
   if (wavelength <= kLambdaMinCie || wavelength >= kLambdaMaxCie) return 0.0;
   double u = (wavelength - kLambdaMinCie) / 5.0;
-  int row = (int)std::floor(u);
+  int row = (int)om::floor(u);
   u -= row;
   return kCie[row][column] * (1.0 - u) + kCie[row + 1][column] * u;
 }
@@ -1272,9 +1290,9 @@ void oracle_radiance_to_luminance_factors(const double* wavelengths, const doubl
     double g_bar = m[3] * x_bar + m[4] * y_bar + m[5] * z_bar;
     double b_bar = m[6] * x_bar + m[7] * y_bar + m[8] * z_bar;
     double irradiance = oracle_interpolate(wavelengths, solar, n, lambda);
-    k[0] += r_bar * irradiance / solar_r * std::pow(lambda / lr, lambda_power);
-    k[1] += g_bar * irradiance / solar_g * std::pow(lambda / lg, lambda_power);
-    k[2] += b_bar * irradiance / solar_b * std::pow(lambda / lb, lambda_power);
+    k[0] += r_bar * irradiance / solar_r * om::pow(lambda / lr, lambda_power);
+    k[1] += g_bar * irradiance / solar_g * om::pow(lambda / lg, lambda_power);
+    k[2] += b_bar * irradiance / solar_b * om::pow(lambda / lb, lambda_power);
   }
   for (int i = 0; i < 3; ++i) k[i] *= kMaxLuminousEfficacy * dlambda;
 }

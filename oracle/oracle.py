@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libatmo_oracle.so")
 ORACLE_GPU_SO = os.path.join(HERE, "_build", "libatmo_oracle_gpu.so")
+ORACLE_COUNT_SO = os.path.join(HERE, "_build", "libatmo_oracle_count.so")
 REF_SO = os.path.join(HERE, "_ref", "libatmo_ref.so")
 
 
@@ -285,6 +286,117 @@ def gpu_precompute(atm: Atmosphere, shp, orders=4, lum=None, blend=False, combin
     if rc != 0:
         raise RuntimeError("GPU oracle precompute failed")
     return out
+
+
+_count = None
+
+# Operation kinds and buckets of the FLOP-counting build (atmo_oracle_count.cc).
+COUNT_OPS = ("add", "mul", "div", "sqrt", "exp", "pow", "sin", "cos", "floor", "fmod", "cmp")
+COUNT_PASSES = ("transmittance", "direct_irradiance", "single_scattering",
+                "scattering_density", "indirect_irradiance", "multiple_scattering", "host")
+
+
+def count_lib():
+    """The oracle compiled with a counting scalar type (atmo_oracle_count.cc);
+    built on first use."""
+    global _count
+    if _count is None:
+        src = os.path.join(HERE, "atmo_oracle_count.cc")
+        deps = [src, os.path.join(HERE, "atmo_oracle.cc"), os.path.join(HERE, "atmo_oracle.h")]
+        if (not os.path.exists(ORACLE_COUNT_SO) or
+                os.path.getmtime(ORACLE_COUNT_SO) < max(map(os.path.getmtime, deps))):
+            os.makedirs(os.path.dirname(ORACLE_COUNT_SO), exist_ok=True)
+            subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC",
+                                   "-shared", "-pthread", src, "-o", ORACLE_COUNT_SO])
+        L = C.CDLL(ORACLE_COUNT_SO)
+        L.oracle_precompute.restype = C.c_int
+        L.oracle_precompute.argtypes = [P(Atmosphere), P(Shape), C.c_uint, dp, C.c_int, C.c_int,
+                                        C.c_int, dp, dp, dp, dp]
+        L.oracle_time_precompute_sample.restype = C.c_int
+        L.oracle_time_precompute_sample.argtypes = [P(Atmosphere), P(Shape), C.c_uint, C.c_int,
+                                                    C.c_int, dp]
+        L.oracle_count_reset.argtypes = []
+        L.oracle_count_dims.argtypes = [P(C.c_int)]
+        L.oracle_count_read.argtypes = [P(C.c_ulonglong), P(C.c_ulonglong)]
+        _count = L
+    return _count
+
+
+def _read_counts(L):
+    dims = (C.c_int * 3)()
+    L.oracle_count_dims(dims)
+    nb, nf, no = dims
+    assert (nb, nf, no) == (len(COUNT_PASSES), 2, len(COUNT_OPS))
+    counts = np.zeros(nb * nf * no, np.uint64)
+    calls = np.zeros(nb, np.uint64)
+    L.oracle_count_read(counts.ctypes.data_as(P(C.c_ulonglong)),
+                        calls.ctypes.data_as(P(C.c_ulonglong)))
+    counts = counts.reshape(nb, nf, no)
+    out = {}
+    for b, name in enumerate(COUNT_PASSES):
+        out[name] = {"texels": int(calls[b]),
+                     "shader": {op: int(counts[b, 0, o]) for o, op in enumerate(COUNT_OPS)},
+                     "filter": {op: int(counts[b, 1, o]) for o, op in enumerate(COUNT_OPS)}}
+    return out
+
+
+def count_ops(atm: Atmosphere, shp, orders=4, lum=None, blend=False, combined=True,
+              threads=0, stride=1, out: Luts | None = None):
+    """Runs precompute() through the counting build and returns, per pass, the
+    texel evaluations and the operations by kind, shader arithmetic and texture
+    filtering apart.  stride > 1 evaluates every stride-th texel of the
+    density and multiple-scattering passes only (a sample, identity luminance,
+    separate single Mie; their per-texel averages stand for the full pass).
+    With stride 1 the LUTs (in `out`) equal precompute()'s; with combined
+    textures no single-Mie table is written, as in the reference."""
+    if not isinstance(shp, Shape):
+        shp = shape(*shp)
+    L = count_lib()
+    L.oracle_count_reset()
+    if stride > 1:
+        seconds = np.zeros(6)
+        rc = L.oracle_time_precompute_sample(C.byref(atm), C.byref(shp), orders, stride,
+                                             threads, _arr(seconds))
+    else:
+        out = out or Luts(shp)
+        lum = np.ascontiguousarray(IDENTITY if lum is None
+                                   else np.asarray(lum, np.float64).reshape(9))
+        rc = L.oracle_precompute(C.byref(atm), C.byref(shp), orders, _arr(lum), int(blend),
+                                 int(combined), threads, _arr(out.transmittance),
+                                 _arr(out.scattering),
+                                 _arr(None if combined else out.single_mie),
+                                 _arr(out.irradiance))
+    if rc != 0:
+        raise RuntimeError("counting oracle precompute failed: %d" % rc)
+    return _read_counts(L)
+
+
+def count_texels(atm: Atmosphere, shp, kind, order, idx, threads=0):
+    """The operations of evaluating texels idx of pass `kind` (0 transmittance,
+    1 direct irradiance, 2 single scattering, 3 scattering density, 4 indirect
+    irradiance, 5 multiple scattering; `order` as the pass takes it) through
+    the counting build, as count_ops() reports one pass.  The input LUTs hold
+    ones: no branch of the evaluators depends on LUT values, only on the
+    geometry, so the counts are those of the real pass at these texels."""
+    if not isinstance(shp, Shape):
+        shp = shape(*shp)
+    L = count_lib()
+    if not hasattr(L, "_eval_sig"):
+        L.oracle_eval_texels.restype = None
+        L.oracle_eval_texels.argtypes = [C.c_int, P(Atmosphere), P(Shape), dp, dp, dp, dp, dp,
+                                         dp, C.c_int, C.c_int, P(C.c_longlong), dp, dp, C.c_int]
+        L._eval_sig = True
+    T = np.ones(shp.t_size * 4)
+    S = np.ones(shp.s_size * 4)
+    I = np.ones(shp.i_size * 4)
+    idx = np.ascontiguousarray(idx, np.int64)
+    out = np.zeros(4 * len(idx))
+    out2 = np.zeros(4 * len(idx))
+    L.oracle_count_reset()
+    L.oracle_eval_texels(kind, C.byref(atm), C.byref(shp), _arr(T), _arr(S), _arr(S), _arr(S),
+                         _arr(I), _arr(S), order, len(idx),
+                         idx.ctypes.data_as(P(C.c_longlong)), _arr(out), _arr(out2), threads)
+    return _read_counts(L)[COUNT_PASSES[kind]]
 
 
 def ref_lib():
