@@ -248,17 +248,15 @@ bool DensityFastFits(const Shape& s) { return DensityBaseSmem(s, 2) <= 48 * 1024
 template <bool kOrder2>
 __host__ __device__ constexpr int DensityTexelsPerTask() { return 4; }
 
-// Above order 2 the outgoing direction's phase functions and the scattering
-// coefficients fold into one weight per channel and direction (shared by the
-// task's 4 texels); at order 2 the Rayleigh and Mie sums stay apart (the
-// ground term joins after the single-scattering phase functions).
+// The outgoing direction's phase functions and the scattering coefficients
+// fold into one weight per channel and direction, shared by the task's 4
+// texels (one mu row: one altitude), so a texel keeps one sum.
 template <bool kOrder2>
 struct DensityTask {
   static constexpr int kN = DensityTexelsPerTask<kOrder2>();
   using V = std::conditional_t<kOrder2, F3, P3>;   // packed above order 2
   float sx[kN], sy[kN];   // the sun's x, y
-  V sum[kN];              // order 2: sums of L P_R(nu2) dw; else L (a_R P_R + a_M P_M) dw
-  F3 sum_m[kOrder2 ? kN : 1];   // order 2: sums of L P_M(nu2) dw
+  V sum[kN];              // sums of L (a_R P_R(nu2) + a_M P_M(nu2)) dw
 };
 
 // The 32 phi samples of theta row l for the texels of one task.  Everything
@@ -295,9 +293,8 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
     const float nu2 = fmaf(oxs, cs.x, B);
     const float q2 = fmaf(nu2, nu2, 1.0f);
     const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
-    // Order 2: war.x = wam.x = dw.
-    const float pr = kOrder2 ? q2 * war.x : 0.0f, pm = kOrder2 ? pr * (rs * rs * rs) : 0.0f;
-    const P3 w = ToP3(kOrder2 ? f3(0.0f) : fma3(wam, q2 * (rs * rs * rs), war * q2));
+    const F3 wf = fma3(wam, q2 * (rs * rs * rs), war * q2);
+    const P3 w = ToP3(wf);
     const float hc = cs.x * hs, hn = cs.y * hs;
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
@@ -350,8 +347,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
         }
       }
       if constexpr (kOrder2) {
-        task.sum[q] = fma3(Ls, pr, task.sum[q]);
-        task.sum_m[q] = fma3(Ls, pm, task.sum_m[q]);
+        task.sum[q] = fma3(Ls, wf, task.sum[q]);
       } else {
         task.sum[q] = Fma(Ls, w, task.sum[q]);
       }
@@ -508,15 +504,10 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       task.sx[q] = ang.sx;
       task.sy[q] = ang.sy;
       task.sum[q] = typename DensityTask<kOrder2>::V{};
-      task.sum_m[kOrder2 ? q : 0] = f3(0.0f);
     }
-    // The scattering coefficients at the texel, with the phase constants
-    // (order 2 applies them after the loop, which saves their registers).
-    F3 a_r = f3(0.0f), a_m = f3(0.0f);
-    if (!kOrder2) {
-      a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
-      a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
-    }
+    // The scattering coefficients at the texel, with the phase constants.
+    const F3 a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
+    const F3 a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
     // Order 2: the ground point's mu_g = (r mu_s + dist nu1) / Rb; its
     // irradiance coordinate 1/2 + kg mu_g is w0 + kg dist nu1 / Rb.
     const float w0 = fmaf(row.r * cc.mu_s * inv_rb, kg, 0.5f);
@@ -536,8 +527,8 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
           // w0 + kg dist (s - 1/2) / (k1 Rb).
           const float gs = kg * dr.dist_ground * inv_rb * inv_k1;
           const float go = fmaf(-0.5f, gs, w0);
-          DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, f3(dw), f3(dw), fnu, inv_k1,
-                                         row_adj, f3(dr.t_ground), gs, go, fiw, ir_adj);
+          DensityThetaRow<kOrder2, true>(task, c, A, hs, B, oxs, a_r * dw, a_m * dw, fnu,
+                                         inv_k1, row_adj, f3(dr.t_ground), gs, go, fiw, ir_adj);
         } else {
           const MergeRow mr = meta[l];
           if (mr.jstride != 0) {
@@ -551,20 +542,14 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
           }
         }
       } else {
-        DensityThetaRow<kOrder2, false>(task, c, A, hs, B, oxs, kOrder2 ? f3(dw) : a_r * dw,
-                                        kOrder2 ? f3(dw) : a_m * dw, fnu, inv_k1, row_adj,
-                                        f3(0.0f), 0.0f, 0.0f, fiw, ir_adj);
+        DensityThetaRow<kOrder2, false>(task, c, A, hs, B, oxs, a_r * dw, a_m * dw, fnu, inv_k1,
+                                        row_adj, f3(0.0f), 0.0f, 0.0f, fiw, ir_adj);
       }
-    }
-    if (kOrder2) {
-      a_r = c.rayleigh * (ProfileDensity(c.prof_r, row.h) * c.ray_k);
-      a_m = c.mie_sca * (ProfileDensity(c.prof_m, row.h) * c.mie_k);
     }
 #pragma unroll
     for (int q = 0; q < kDensityTexelsPerTask; ++q) {
       if (n0 + q < NU) {
-        const F3 J =
-            kOrder2 ? a_r * ToF3(task.sum[q]) + a_m * task.sum_m[q] : ToF3(task.sum[q]);
+        const F3 J = ToF3(task.sum[q]);
         in.dJ[(k * s.smu + j) * W + (n0 + q) * s.smus + col] = to4(J, 1.0f);
       }
     }
