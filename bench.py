@@ -124,7 +124,11 @@ def dist_info():
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (FP64 restatement of the reference CPU model).
 # ---------------------------------------------------------------------------
-def cpu_rebuild_seconds(stride=16, threads=0):
+def cpu_rebuild_seconds(stride=16, threads=0, by_rows=False):
+    """One rebuild by the FP64 oracle, density and multiple scattering sampled
+    on every stride-th texel and scaled.  by_rows: the threads take whole rows
+    and r-slices (the reference CPU driver's partition) instead of 64-texel
+    blocks."""
     from oracle import oracle as O
     O.build()
     import ctypes as C
@@ -132,8 +136,9 @@ def cpu_rebuild_seconds(stride=16, threads=0):
     shp = O.shape(*O.DEFAULT_SHAPE)
     sec = np.zeros(6)
     t0 = time.perf_counter()
-    rc = O.lib().oracle_time_precompute_sample(C.byref(atm), C.byref(shp), 4, stride, threads,
-                                               sec.ctypes.data_as(O.dp))
+    rc = O.lib().oracle_time_precompute_partitioned(C.byref(atm), C.byref(shp), 4, stride,
+                                                    threads, int(by_rows),
+                                                    sec.ctypes.data_as(O.dp))
     wall = time.perf_counter() - t0
     if rc != 0:
         raise RuntimeError("oracle timing failed")
@@ -145,12 +150,18 @@ def cpu_rebuild_seconds(stride=16, threads=0):
 def cpu_baseline_entry(stride=16):
     cores = os.cpu_count() or 1
     full, wall, sec = cpu_rebuild_seconds(stride)
+    rows_full, rows_wall, _ = cpu_rebuild_seconds(stride, by_rows=True)
     return {"value": 1.0 / full, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": ("one config-0 Earth rebuild (4 orders) by the FP64 oracle with %d threads; "
-                       "transmittance, irradiance and single scattering in full, scattering "
-                       "density and multiple scattering on every %dth texel and scaled x%d "
-                       "(%.1f s of CPU wall time, extrapolated rebuild %.1f s)"
-                       % (cores, stride, stride, wall, full))}
+            "sample": ("one config-0 Earth rebuild (4 orders) by the FP64 oracle with %d threads "
+                       "taking 64-texel blocks; transmittance, irradiance and single scattering "
+                       "in full, scattering density and multiple scattering on every %dth texel "
+                       "and scaled x%d (%.1f s of CPU wall time, extrapolated rebuild %.1f s)"
+                       % (cores, stride, stride, wall, full)),
+            "reference_partition": {
+                "value": 1.0 / rows_full, "unit": UNIT,
+                "partition": "whole texture rows and r-slices per thread, as the reference's "
+                             "CPU driver (atmosphere/reference/model.cc:140-237) hands them to "
+                             "RunJobs; the same sample (%.1f s wall)" % rows_wall}}
 
 
 def run_reference(args):
@@ -167,6 +178,7 @@ def run_reference(args):
         totals.append(full)
     wall = time.perf_counter() - t0
     value = len(totals) / sum(totals)
+    rows_full, _, _ = cpu_rebuild_seconds(stride, by_rows=True)
     cores = os.cpu_count() or 1
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
@@ -177,8 +189,14 @@ def run_reference(args):
                    "CPU oracle port of atmosphere/reference/model.cc (FP64, all host threads)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "per step: one rebuild with density/multiple scattering on "
-                                   "every %dth texel, scaled; %.1f s wall for %d steps"
-                                   % (stride, wall, args.steps)},
+                                   "every %dth texel, scaled, threads taking 64-texel blocks; "
+                                   "%.1f s wall for %d steps" % (stride, wall, args.steps),
+                         "reference_partition": {
+                             "value": 1.0 / rows_full, "unit": UNIT,
+                             "partition": "whole texture rows and r-slices per thread, as the "
+                                          "reference's CPU driver hands them to RunJobs "
+                                          "(atmosphere/reference/model.cc:140-237); one rebuild "
+                                          "of the same sample"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -814,13 +814,15 @@ ORACLE_HD Spec GetSunAndSkyIrradiance(const Atm& a, const Tex2& T, const Tex2& I
 }
 
 // ---------------------------------------------------------------------------
-// Threading: work stealing over blocks of texels (finer than the reference's
-// RunJobs over rows / r-slices, atmosphere/reference/model.cc:140-237).
+// Threading: work stealing over blocks of `chunk` consecutive texels.  The
+// default, 64, is finer than the reference's RunJobs jobs; a texture row
+// (transmittance, irradiance) or an r-slice (scattering) per block is the
+// reference's own partition (atmosphere/reference/model.cc:140-237).
 // ---------------------------------------------------------------------------
 template <typename F>
-void ParallelFor(long long n, int threads, F&& fn) {
+void ParallelFor(long long n, int threads, F&& fn, long long chunk = 64) {
   if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-  const long long chunk = 64;
+  if (chunk < 1) chunk = 1;
   std::atomic<long long> next(0);
   auto worker = [&]() {
     for (;;) {
@@ -924,7 +926,7 @@ ORACLE_HD void EvalTexel(int kind, const Atm& a, const Tex2& T, const Tex3& SR, 
 int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9], bool blend,
                bool combined, int threads, double* transmittance, double* scattering,
                double* single_mie, double* irradiance, int density_stride,
-               double seconds[6]) {
+               double seconds[6], bool by_rows = false) {
   using Clock = std::chrono::steady_clock;
   auto tick = Clock::now();
   auto lap = [&](int slot) {
@@ -943,17 +945,23 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
   Tex3 DR = MakeS(a, dR.data()), DM = MakeS(a, dM.data()), DJ = MakeS(a, dJ.data()),
        DMulti = MakeS(a, dMulti.data());
   Tex3 none{1, 1, 1, nullptr};
+  // Texels per work block: the reference's rows and r-slices, or 64.
+  const long long slice = (long long)a.S_NU * a.S_MU_S * a.S_MU;
+  const int stride = density_stride > 1 ? density_stride : 1;
+  const long long chunk_T = by_rows ? a.T_W : 64, chunk_I = by_rows ? a.I_W : 64;
+  const long long chunk_S = by_rows ? slice : 64;
+  const long long chunk_sampled = by_rows ? std::max(1LL, slice / stride) : 64;
 
   // Transmittance (model.cc:1085-1091).
   ParallelFor(nT, threads, [&](long long i) {
     EvalTexel(0, a, T, none, none, none, DI, none, 0, i, transmittance + 4 * i, nullptr);
-  });
+  }, chunk_T);
   lap(0);
   // Direct irradiance; irradiance is zeroed unless blending (model.cc:1093-1106).
   ParallelFor(nI, threads, [&](long long i) {
     EvalTexel(1, a, T, none, none, none, DI, none, 0, i, dI.data() + 4 * i, nullptr);
     if (!blend) Store(irradiance + 4 * i, Spec(0.0), 0.0);
-  });
+  }, chunk_I);
   lap(1);
   // Single scattering (model.cc:1108-1134, shader model.cc:142-157).
   ParallelFor(nS, threads, [&](long long i) {
@@ -975,7 +983,7 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
         Store(m, lmie, 0.0);
       }
     }
-  });
+  }, chunk_S);
   lap(2);
   for (unsigned order = 2; order <= num_scattering_orders; ++order) {
     // Scattering density (model.cc:1140-1166).  The reference aliases
@@ -986,13 +994,13 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
       ParallelFor(nS, threads, [&](long long i) {
         EvalTexel(3, a, T, DR, DM, multi_in, DI, none, (int)order, i, dJ.data() + 4 * i,
                   nullptr);
-      });
+      }, chunk_S);
     } else {
       ParallelFor(nS / density_stride, threads, [&](long long i) {
         long long t = i * density_stride;
         EvalTexel(3, a, T, DR, DM, multi_in, DI, none, (int)order, t, dJ.data() + 4 * t,
                   nullptr);
-      });
+      }, chunk_sampled);
     }
     lap(3);
     // Indirect irradiance with order - 1 (model.cc:1168-1189).
@@ -1000,7 +1008,7 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
     ParallelFor(nI, threads, [&](long long i) {
       EvalTexel(4, a, T, DR, DM, multi_in, DI, none, (int)order - 1, i, newI.data() + 4 * i,
                 nullptr);
-    });
+    }, chunk_I);
     dI.swap(newI);
     DI.p = dI.data();
     ORACLE_COUNT_PASS(4);
@@ -1020,9 +1028,10 @@ int Precompute(const Atm& a, unsigned num_scattering_orders, const double lum[9]
       Store(s, Spec::From(s) + add, s[3]);
     };
     if (density_stride <= 1) {
-      ParallelFor(nS, threads, ms);
+      ParallelFor(nS, threads, ms, chunk_S);
     } else {
-      ParallelFor(nS / density_stride, threads, [&](long long i) { ms(i * density_stride); });
+      ParallelFor(nS / density_stride, threads, [&](long long i) { ms(i * density_stride); },
+                  chunk_sampled);
     }
     lap(5);
   }
@@ -1236,9 +1245,9 @@ int oracle_precompute(const oracle_atmosphere* a, const oracle_shape* s,
                     transmittance, scattering, single_mie, irradiance, 1, nullptr);
 }
 
-int oracle_time_precompute_sample(const oracle_atmosphere* a, const oracle_shape* s,
-                                  unsigned num_scattering_orders, int stride, int threads,
-                                  double seconds[6]) {
+int oracle_time_precompute_partitioned(const oracle_atmosphere* a, const oracle_shape* s,
+                                       unsigned num_scattering_orders, int stride, int threads,
+                                       int by_rows, double seconds[6]) {
   Atm at = ToAtm(a, s);
   const long long nT = (long long)at.T_W * at.T_H;
   const long long nI = (long long)at.I_W * at.I_H;
@@ -1247,7 +1256,14 @@ int oracle_time_precompute_sample(const oracle_atmosphere* a, const oracle_shape
   const double id[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   for (int i = 0; i < 6; ++i) seconds[i] = 0.0;
   return Precompute(at, num_scattering_orders, id, false, false, threads, T.data(), S.data(),
-                    M.data(), I.data(), stride, seconds);
+                    M.data(), I.data(), stride, seconds, by_rows != 0);
+}
+
+int oracle_time_precompute_sample(const oracle_atmosphere* a, const oracle_shape* s,
+                                  unsigned num_scattering_orders, int stride, int threads,
+                                  double seconds[6]) {
+  return oracle_time_precompute_partitioned(a, s, num_scattering_orders, stride, threads, 0,
+                                            seconds);
 }
 
 double oracle_interpolate(const double* wavelengths, const double* values, int n,

@@ -156,6 +156,13 @@ int oracle_precompute(const oracle_atmosphere* a, const oracle_shape* s,
 int oracle_time_precompute_sample(const oracle_atmosphere* a, const oracle_shape* s,
                                   unsigned num_scattering_orders, int stride,
                                   int threads, double seconds[6]);
+/* The same with by_rows != 0: the threads take whole texture rows
+   (transmittance, irradiance) and r-slices (scattering) as work items, the
+   partition of the reference's CPU driver (atmosphere/reference/model.cc:
+   140-237), instead of blocks of 64 texels. */
+int oracle_time_precompute_partitioned(const oracle_atmosphere* a, const oracle_shape* s,
+                                       unsigned num_scattering_orders, int stride,
+                                       int threads, int by_rows, double seconds[6]);
 
 /* ---- spectral set-up and render-time functions --------------------------- */
 /* atmosphere/model.cc:535-552 */

@@ -237,6 +237,7 @@ def lib():
                                           P(C.c_longlong), dp, dp, i]),
             "oracle_precompute": (i, [A, S, C.c_uint, dp, i, i, i, dp, dp, dp, dp]),
             "oracle_time_precompute_sample": (i, [A, S, C.c_uint, i, i, dp]),
+            "oracle_time_precompute_partitioned": (i, [A, S, C.c_uint, i, i, i, dp]),
             "oracle_interpolate": (d, [dp, dp, i, d]),
             "oracle_cie_table_value": (d, [d, i]),
             "oracle_radiance_to_luminance_factors": (None, [dp, dp, i, d, dp]),
