@@ -70,6 +70,16 @@ DENSITY_FLOPS_PER_SAMPLE = {2: 48.9, 3: 20.1}
 FLOPS_CONFIG0 = os.path.join(ROOT, "tests", "golden", "flops_config0.json")
 
 
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth of the GB300s, else
+    the recipe's fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "6.8 TB/s (fallback: MEASURED_PEAKS.json absent)"
+
+
 def reference_flops():
     with open(FLOPS_CONFIG0) as f:
         d = json.load(f)
@@ -444,6 +454,8 @@ def roofline_entry(batch, B, peak, stream, rebuilds_per_s):
     executed = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
     executed_rate = executed / (dens_ms * 1e-3) / 1e12
     traffic = sum(DENSITY_DRAM_BYTES_PER_INSTANCE[min(o, 3)] * B for o, _ in dens) / len(dens)
+    hbm, hbm_source = hbm_peak()
+    dram_gbs = traffic / (dens_ms / len(dens) * 1e-3) / 1e9
     return {"bound": "fp32", "kernel": "scattering density",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "flops": "the reference algorithm's: adds and muls of ComputeScatteringDensity "
@@ -467,6 +479,8 @@ def roofline_entry(batch, B, peak, stream, rebuilds_per_s):
                               "launch per order (profiles/fast_kernels_earth_default_batch2.md), "
                               "scaled to %d instances; bytes per launch, averaged over the "
                               "step's density launches" % B,
+            "dram": {"bytes_per_launch": traffic, "achieved_gbs": dram_gbs, "peak_gbs": hbm,
+                     "frac": dram_gbs / hbm, "peak_source": hbm_source},
             "peak_source": "FP32 FMA throughput measured in this run by atmo_measure_fp32_peak "
                            "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
             "avg_launch_ms": dens_ms / len(dens), "launches_per_step": len(dens),
