@@ -5,6 +5,7 @@ Tolerances (tests/parity.py): per-texel relative error <= 1e-4 for the
 transmittance LUT and <= 1e-3 for scattering, single-Mie and irradiance, with
 an absolute floor at 1e-6 of each channel's maximum."""
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -114,6 +115,49 @@ def test_odd_sizes_vs_oracle(atmo, oracle, torch, path):
     atm = oracle.earth_atmosphere()
     ref = oracle.precompute(atm, shape, 4, combined=True)
     compare(ref, gpu_precompute(atmo, torch, atm, shape, 4, True, path), True)
+
+
+def density_merge_need_and_room(shape, rb, rt):
+    """The fast density kernel's merged ground tables above order 2: the
+    host's budget estimate (DensityMergeNeed: the worst r-slice's sum over
+    its ground rows of (NU + 1) J entries of 32 bytes) and the room a block
+    has for them (99 KB minus DensityBaseSmem), as atmo_fast.cu computes
+    them."""
+    _, _, sr, _, _, nu, iw, _ = shape
+    h = math.sqrt(rt * rt - rb * rb)
+    k1, kg = (nu - 1) / (2.0 * nu), (iw - 1) / (2.0 * iw)
+    worst = 0
+    for k in range(sr):
+        rho = h * k / max(sr - 1, 1)
+        r = math.sqrt(rho * rho + rb * rb)
+        entries = 0
+        for l in range(16):
+            mu = math.cos((l + 0.5) * math.pi / 16)
+            disc = r * r * (mu * mu - 1.0) + rb * rb
+            if mu >= 0.0 or disc < 0.0:
+                continue
+            gs = kg * (-r * mu - math.sqrt(disc)) / (rb * k1)
+            entries += (nu + 1) * min(int(math.floor(gs * iw)) + 3, iw + 1)
+        worst = max(worst, entries)
+    base = 16 * (nu + 1) * 32 + (iw + 1) * 32 + (16 * nu + iw) * 16 + 16 * 32 + 16
+    return worst * 32, 99 * 1024 - base
+
+
+@pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
+def test_partially_merged_ground_tables_vs_oracle(atmo, oracle, torch, path):
+    """A small planet under a thick atmosphere (3000 km, 120 km) with a wide
+    irradiance row (256 texels): the grazing ground rays reach many
+    irradiance entries, so above order 2 the merged sky + ground tables of
+    the top r-slices exceed a block's shared memory.  The first ground rows
+    (in theta order) get merged tables; the rest keep the separate sky and
+    ground lookups, in the same block."""
+    shape = (64, 16, 4, 16, 8, 16, 256, 4)
+    need, room = density_merge_need_and_room(shape, 3000.0, 3120.0)
+    assert need > room > 0, (need, room)
+    atm = oracle.earth_atmosphere()
+    atm.bottom_radius, atm.top_radius = 3000.0, 3120.0
+    gpu = gpu_precompute(atmo, torch, atm, shape, 4, True, path)
+    compare_robust(oracle, atm, shape, 4, gpu, True)
 
 
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
