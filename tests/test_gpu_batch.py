@@ -4,7 +4,7 @@ the LUTs it produces alone, and agree with the oracle."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import compare_robust, gpu_precompute, random_atmosphere
+from test_gpu_parity import compare, compare_robust, gpu_precompute, random_atmosphere
 
 pytestmark = pytest.mark.gpu
 
@@ -40,6 +40,22 @@ def test_batch_uneven_equals_alone_and_oracle(atmo, oracle, torch):
         np.testing.assert_array_equal(I, alone[3])
         if i < 3:
             compare_robust(oracle, atms[i], shapes[i], orders[i], [T, S, None, I], True)
+
+
+def test_batch_pass_falls_back_for_every_member(atmo, oracle, torch):
+    """A member whose single-scattering line exceeds the fast kernel's
+    buffers (a 2048-texel transmittance row) makes the batch's
+    single-scattering launch plain for every member (one launch serves them
+    all); each member still matches the oracle, every texel."""
+    atm = oracle.earth_atmosphere()
+    shapes = [(64, 16, 4, 16, 8, 4, 16, 4), (2048, 4, 4, 16, 8, 8, 16, 4)]
+    b = atmo.Batch([atm, atm], shapes, [4, 3], combined=True)
+    b.run()
+    atmo.synchronize_stream()
+    for i, (shape, orders) in enumerate(zip(shapes, [4, 3])):
+        luts = [b.read(i, atmo.LUT_TRANSMITTANCE), b.read(i, atmo.LUT_SCATTERING), None,
+                b.read(i, atmo.LUT_IRRADIANCE)]
+        compare(oracle.precompute(atm, shape, orders, combined=True), luts, True)
 
 
 def test_batch_replay_and_parameter_update(atmo, oracle, torch):

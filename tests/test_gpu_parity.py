@@ -160,6 +160,20 @@ def test_partially_merged_ground_tables_vs_oracle(atmo, oracle, torch, path):
     compare_robust(oracle, atm, shape, 4, gpu, True)
 
 
+@pytest.mark.parametrize("shape", [(64, 16, 2, 4, 16, 128, 16, 4), (2048, 4, 4, 16, 8, 8, 16, 4)],
+                         ids=["line_2048", "transmittance_2048"])
+def test_wide_lines_vs_oracle(atmo, oracle, torch, shape):
+    """The fast path with passes too wide for its restructured kernels: a
+    2048-column scattering line (NU 128 x MU_S 16) exceeds the single- and
+    multiple-scattering kernels' 1024 columns (and NU 128 the density tables'
+    48 KB), and a 2048-texel transmittance row exceeds single scattering's
+    48 KB of line buffers.  Those passes run the plain kernels, the others
+    the fast ones.  Every texel, no mask."""
+    atm = oracle.earth_atmosphere()
+    ref = oracle.precompute(atm, shape, 4, combined=True)
+    compare(ref, gpu_precompute(atmo, torch, atm, shape, 4, True, 0), True)
+
+
 @pytest.mark.parametrize("path", [0, 1], ids=["fast", "plain"])
 @pytest.mark.parametrize("combined", [True, False], ids=["combined", "separate"])
 def test_default_shape_every_texel_vs_gpu_oracle(atmo, oracle, torch, path, combined):
