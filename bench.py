@@ -94,7 +94,7 @@ DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.25e6}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--warm-seconds", type=float, default=8.0,
                    help="keep running untimed steps (at least --warmup) until the GPU has "
@@ -233,7 +233,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
