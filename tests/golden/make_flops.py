@@ -15,7 +15,7 @@ reads a LUT value), so a pass is counted on a systematic sample of its texels
 texels; the luminance products and blending that follow each texel evaluation
 (a constant per texel) are taken from an exact run at the small shape.
 `--exact` also runs the whole configuration-0 precomputation through the
-counting build (~30 min on 8 cores) and records its exact totals beside the
+counting build (~45 min on 8 cores) and records its exact totals beside the
 sampled ones.
 
     python tests/golden/make_flops.py [--exact]
