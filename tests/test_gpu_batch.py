@@ -4,6 +4,7 @@ the LUTs it produces alone, and agree with the oracle."""
 import numpy as np
 import pytest
 
+from parity import TOL_IRRADIANCE, TOL_SCATTERING, TOL_TRANSMITTANCE, check_masked, robust_masks
 from test_gpu_parity import compare, compare_robust, gpu_precompute, random_atmosphere
 
 pytestmark = pytest.mark.gpu
@@ -40,6 +41,29 @@ def test_batch_uneven_equals_alone_and_oracle(atmo, oracle, torch):
         np.testing.assert_array_equal(I, alone[3])
         if i < 3:
             compare_robust(oracle, atms[i], shapes[i], orders[i], [T, S, None, I], True)
+
+
+def test_mixed_shapes_batch_vs_gpu_oracle(atmo, oracle, torch):
+    """The batched configuration's mix in one batch: seeded random planets at
+    the half, default and double-R shapes with 2-6 orders, combined textures.
+    Each member, every texel where the FP64 values are not rounding-dominated
+    (masks from the FP64 GPU oracle), against the FP64 GPU oracle."""
+    from precomputed_atmospheric_scattering_gb300.workloads import DEFAULT, DOUBLE_R, HALF
+    rng = np.random.default_rng(2024)
+    shapes = [HALF, DEFAULT, DOUBLE_R, HALF]
+    orders = [5, 3, 2, 6]
+    atms = [random_atmosphere(oracle, rng) for _ in shapes]
+    b = atmo.Batch(atms, shapes, orders, combined=True)
+    b.run()
+    atmo.synchronize_stream()
+    for i, (atm, shape, n) in enumerate(zip(atms, shapes, orders)):
+        ref, masks = robust_masks(oracle, atm, shape, n, True, precompute=oracle.gpu_precompute)
+        check_masked("transmittance", b.read(i, atmo.LUT_TRANSMITTANCE), ref.transmittance,
+                     TOL_TRANSMITTANCE, masks["transmittance"])
+        check_masked("scattering", b.read(i, atmo.LUT_SCATTERING), ref.scattering,
+                     TOL_SCATTERING, masks["scattering"], channels=4)
+        check_masked("irradiance", b.read(i, atmo.LUT_IRRADIANCE), ref.irradiance,
+                     TOL_IRRADIANCE, masks["irradiance"])
 
 
 def test_batch_pass_falls_back_for_every_member(atmo, oracle, torch):
