@@ -158,6 +158,23 @@ def toy_atmosphere():
         absorption_extinction=(0.0, 0.0, 0.0), ground_albedo=(0.1, 0.0, 0.0), mu_s_min=-1.0)
 
 
+def reference_dir():
+    """The reference's source checkout, or None: ATMO_REFERENCE_DIR when set
+    (it must then hold atmosphere/functions.glsl), else a checkout named
+    `reference` beside this repository's directory when there is one.  The
+    GPU host has neither, and the oracle then runs without the reference
+    build."""
+    env = os.environ.get("ATMO_REFERENCE_DIR")
+    if env:
+        if not os.path.isfile(os.path.join(env, "atmosphere", "functions.glsl")):
+            raise RuntimeError("ATMO_REFERENCE_DIR=%s holds no atmosphere/functions.glsl" % env)
+        return env
+    sibling = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    if os.path.isfile(os.path.join(sibling, "atmosphere", "functions.glsl")):
+        return sibling
+    return None
+
+
 def build(quiet=True):
     """Compiles the oracle restatement (and, when the reference sources are
     present, the reference's own functions.glsl) for this machine."""
@@ -177,8 +194,8 @@ def build(quiet=True):
         subprocess.check_call(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2",
                                "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
                                gpu_src, "-o", ORACLE_GPU_SO])
-    ref_src = os.environ.get("ATMO_REFERENCE_DIR", "/root/reference")
-    if os.path.isdir(os.path.join(ref_src, "atmosphere")):
+    ref_src = reference_dir()
+    if ref_src is not None:
         subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"),
                                "REFERENCE=" + ref_src],
                               stdout=subprocess.DEVNULL if quiet else None)
