@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(atmo):
     L = C.CDLL(atmo.LIB_PATH)
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert L.atmo_abi_version() == 2
+    assert L.atmo_abi_version() == 3
 
 
 def earth_model(atmo, n_lambda=3, combined=True, half=False, shape=None):
@@ -117,21 +117,118 @@ def test_convert_spectrum_to_linear_srgb_matches_oracle(atmo, oracle):
     np.testing.assert_allclose(got, exp, rtol=1e-12)
 
 
-def test_shader_source_header(atmo):
-    m = earth_model(atmo)
+def reference_glsl_header(w, solar, sun_angular_radius, bottom, top, ray_layers, ray_sca,
+                          mie_layers, mie_sca, mie_ext, g, abs_layers, abs_ext, albedo,
+                          max_sun_zenith, unit, n_lambda, combined, shape, sky_k, sun_k):
+    """A restatement of the reference's GLSL header factory
+    (atmosphere/model.cc:636-744) for lambdas = kLambdaR/G/B, with the two
+    GLSL files it splices in (definitions.glsl, functions.glsl) replaced by
+    the marker lines the library writes in their place.  std::to_string of a
+    double is printf's "%f"."""
+    def interpolate(values, lam):            # atmosphere/model.cc:535-552
+        if lam < w[0]:
+            return values[0]
+        for i in range(len(w) - 1):
+            if lam < w[i + 1]:
+                u = (lam - w[i]) / (w[i + 1] - w[i])
+                return values[i] * (1.0 - u) + values[i + 1] * u
+        return values[-1]
+
+    f = lambda x: "%f" % x                   # noqa: E731
+    lambdas = (680.0, 550.0, 440.0)
+
+    def to_string(v, scale):
+        return "vec3(" + ",".join(f(interpolate(v, l) * scale) for l in lambdas) + ")"
+
+    def layer(x):
+        width, exp_term, exp_scale, linear_term, constant_term = x
+        return "DensityProfileLayer(%s,%s,%s,%s,%s)" % (
+            f(width / unit), f(exp_term), f(exp_scale * unit), f(linear_term * unit),
+            f(constant_term))
+
+    def profile(layers):
+        layers = [(0.0, 0.0, 0.0, 0.0, 0.0)] * (2 - len(layers)) + list(layers)
+        return "DensityProfile(DensityProfileLayer[2](" + layer(layers[0]) + "," + \
+            layer(layers[1]) + "))"
+
+    tw, th, sr, smu, smus, snu, iw, ih = shape
+    return ("#version 330\n#define IN(x) const in x\n#define OUT(x) out x\n"
+            "#define TEMPLATE(x)\n#define TEMPLATE_ARGUMENT(x)\n#define assert(x)\n"
+            "const int TRANSMITTANCE_TEXTURE_WIDTH = %d;\n"
+            "const int TRANSMITTANCE_TEXTURE_HEIGHT = %d;\n"
+            "const int SCATTERING_TEXTURE_R_SIZE = %d;\n"
+            "const int SCATTERING_TEXTURE_MU_SIZE = %d;\n"
+            "const int SCATTERING_TEXTURE_MU_S_SIZE = %d;\n"
+            "const int SCATTERING_TEXTURE_NU_SIZE = %d;\n"
+            "const int IRRADIANCE_TEXTURE_WIDTH = %d;\n"
+            "const int IRRADIANCE_TEXTURE_HEIGHT = %d;\n" % (tw, th, sr, smu, smus, snu, iw, ih) +
+            ("#define COMBINED_SCATTERING_TEXTURES\n" if combined else "") +
+            "// <atmosphere/definitions.glsl of the reference goes here>\n" +
+            "const AtmosphereParameters ATMOSPHERE = AtmosphereParameters(\n" +
+            to_string(solar, 1.0) + ",\n" + f(sun_angular_radius) + ",\n" +
+            f(bottom / unit) + ",\n" + f(top / unit) + ",\n" + profile(ray_layers) + ",\n" +
+            to_string(ray_sca, unit) + ",\n" + profile(mie_layers) + ",\n" +
+            to_string(mie_sca, unit) + ",\n" + to_string(mie_ext, unit) + ",\n" + f(g) + ",\n" +
+            profile(abs_layers) + ",\n" + to_string(abs_ext, unit) + ",\n" +
+            to_string(albedo, 1.0) + ",\n" + f(math.cos(max_sun_zenith)) + ");\n" +
+            "const vec3 SKY_SPECTRAL_RADIANCE_TO_LUMINANCE = vec3(%s,%s,%s);\n" % tuple(
+                f(x) for x in sky_k) +
+            "const vec3 SUN_SPECTRAL_RADIANCE_TO_LUMINANCE = vec3(%s,%s,%s);\n" % tuple(
+                f(x) for x in sun_k) +
+            "// <atmosphere/functions.glsl of the reference goes here>\n")
+
+
+@pytest.mark.parametrize("n_lambda,combined", [(3, True), (15, False)])
+def test_shader_source_header_is_the_reference_header(atmo, oracle, n_lambda, combined):
+    """The generated header, byte for byte, against the restatement of
+    model.cc:636-744 for the same constructor arguments (3 wavelengths with
+    combined textures: the radiance API; 15 wavelengths with a separate
+    single-Mie texture: precomputed luminance, SKY_..._TO_LUMINANCE = 683)."""
+    w = np.arange(360.0, 831.0, 10.0)
+    lam = w * 1e-3
+    mie = 5.328e-3 / 1200.0 * np.ones_like(w)
+    m = earth_model(atmo, n_lambda=n_lambda, combined=combined)
+    solar = np.full_like(w, 1.5)
+    sun_k = np.zeros(3)
+    L = oracle.lib()
+    L.oracle_radiance_to_luminance_factors(w.ctypes.data_as(oracle.dp),
+                                           solar.ctypes.data_as(oracle.dp), len(w), 0.0,
+                                           sun_k.ctypes.data_as(oracle.dp))
+    if n_lambda > 3:
+        sky_k = np.full(3, 683.0)
+    else:
+        sky_k = np.zeros(3)
+        L.oracle_radiance_to_luminance_factors(w.ctypes.data_as(oracle.dp),
+                                               solar.ctypes.data_as(oracle.dp), len(w), -3.0,
+                                               sky_k.ctypes.data_as(oracle.dp))
+    xs = np.array([1.18e-27, 2.182e-28, 2.818e-28, 6.636e-28, 1.527e-27, 2.763e-27, 5.52e-27,
+                   8.451e-27, 1.582e-26, 2.316e-26, 3.669e-26, 4.924e-26, 7.752e-26, 9.016e-26,
+                   1.48e-25, 1.602e-25, 2.139e-25, 2.755e-25, 3.091e-25, 3.5e-25, 4.266e-25,
+                   4.672e-25, 4.398e-25, 4.701e-25, 5.019e-25, 4.305e-25, 3.74e-25, 3.215e-25,
+                   2.662e-25, 2.238e-25, 1.852e-25, 1.473e-25, 1.209e-25, 9.423e-26, 7.455e-26,
+                   6.566e-26, 5.105e-26, 4.15e-26, 4.228e-26, 3.237e-26, 2.451e-26, 2.801e-26,
+                   2.534e-26, 1.624e-26, 1.465e-26, 2.078e-26, 1.383e-26, 7.105e-27])
+    want = reference_glsl_header(
+        list(w), list(solar), 0.00935 / 2.0, 6360e3, 6420e3, [(0.0, 1.0, -1.0 / 8000.0, 0.0, 0.0)],
+        list(1.24062e-6 * lam ** -4), [(0.0, 1.0, -1.0 / 1200.0, 0.0, 0.0)], list(mie * 0.9),
+        list(mie), 0.8, [(25000.0, 0.0, 0.0, 1.0 / 15000.0, -2.0 / 3.0),
+                         (0.0, 0.0, 0.0, -1.0 / 15000.0, 8.0 / 3.0)],
+        list(300.0 * 2.687e20 / 15000.0 * xs), list(np.full_like(w, 0.1)),
+        102.0 / 180.0 * math.pi, 1000.0, n_lambda, combined, atmo.DEFAULT_SHAPE, sky_k, sun_k)
     src = m.shader()
-    assert src.startswith("#version 330\n")
-    assert "const int SCATTERING_TEXTURE_MU_SIZE = 128;" in src
-    assert "#define COMBINED_SCATTERING_TEXTURES" in src
-    assert "vec3(0.005802,0.013558,0.033100)" in src
-    assert "#define RADIANCE_API_ENABLED" in src
+    assert src[:len(want)] == want
+    # Then the API shader of model.cc:221-281 (the radiance API only below 4
+    # precomputed wavelengths).
+    api = src[len(want):]
+    assert api.startswith("#define RADIANCE_API_ENABLED\n") == (n_lambda <= 3)
+    for fn in ("GetSolarLuminance", "GetSkyLuminance", "GetSkyLuminanceToPoint",
+               "GetSunAndSkyIlluminance"):
+        assert fn + "(" in api
+    # The radiance functions sit between #ifdef RADIANCE_API_ENABLED and #endif.
+    guarded = api[api.index("#ifdef RADIANCE_API_ENABLED\n"):api.index("#endif\n")]
     for fn in ("GetSolarRadiance", "GetSkyRadiance", "GetSkyRadianceToPoint",
-               "GetSunAndSkyIrradiance", "GetSolarLuminance", "GetSkyLuminance",
-               "GetSkyLuminanceToPoint", "GetSunAndSkyIlluminance"):
-        assert fn + "(" in src
-    src15 = earth_model(atmo, n_lambda=15, combined=False).shader()
-    assert "#define RADIANCE_API_ENABLED" not in src15
-    assert "COMBINED_SCATTERING_TEXTURES" not in src15
+               "GetSunAndSkyIrradiance"):
+        assert fn + "(" in guarded
 
 
 def test_set_program_uniforms_is_unavailable(atmo):
