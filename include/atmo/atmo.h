@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ATMO_ABI_VERSION 2
+#define ATMO_ABI_VERSION 3
 
 #define ATMO_LAMBDA_R 680.0
 #define ATMO_LAMBDA_G 550.0
@@ -59,7 +59,8 @@ typedef enum {
   ATMO_TIMEOUT = 4,       /* a bounded wait ran out */
   ATMO_BUDGET = 5,        /* the request does not fit the device-memory budget */
   ATMO_UNAVAILABLE = 6,   /* feature not available here (e.g. OpenGL interop) */
-  ATMO_NOT_READY = 7      /* LUTs requested before Init */
+  ATMO_NOT_READY = 7,     /* LUTs requested before Init */
+  ATMO_CANCELLED = 8      /* a serving request cancelled by atmo_server_cancel */
 } atmo_status;
 
 /* atmosphere/model.h:165-178: density = exp_term*exp(exp_scale*h)
@@ -235,14 +236,59 @@ atmo_status atmo_precompute(const atmo_atmosphere* atmosphere, const atmo_lut_sh
    GPU loading this library holds until exit; shapes needing more (the
    reference's default shape needs ~49 MiB) return ATMO_BUDGET.  All calls
    share that array: calls whose GPU work overlaps race, so serialise them.
-   The first call on each device looks up the array's device address and
-   should come before any stream capture.  Path: ATMO_PATH_FAST. */
+   The array's memory is taken when the library's device code for this entry
+   point loads: with CUDA's default lazy loading, at the first call on each
+   device (make that call, or set CUDA_MODULE_LOADING=EAGER, before reserving
+   all device memory; otherwise it fails with ATMO_OOM).  The first call in
+   each CUDA context looks up the array's device address and should come
+   before any stream capture.  The launch descriptors travel as kernel
+   parameters: a call copies nothing from host memory.  Path: ATMO_PATH_FAST. */
 atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere,
                                     const atmo_lut_shape* shape,
                                     unsigned num_scattering_orders, const float lum[9],
                                     int blend, int combined, float* transmittance,
                                     float* scattering, float* single_mie, float* irradiance,
                                     atmo_stream stream);
+
+/* ---- one pass of the order loop over caller-owned LUTs --------------------- */
+/* The draws of Model::Precompute's order loop (atmosphere/model.cc:1137-1211),
+   one at a time, on float32 RGBA device LUTs the caller fills: an inspection
+   and test hook for the per-pass kernels, e.g. with the uniform radiance,
+   uniform irradiance and unit transmittance under which
+   atmosphere/reference/functions_test.cc:1130-1344 states closed forms.
+     ATMO_PASS_SCATTERING_DENSITY   ComputeScatteringDensityTexture
+       (functions.glsl:1348-1367) of order `order` >= 2: reads
+       delta_rayleigh and delta_mie (single scattering, order 2) or
+       delta_rayleigh (delta multiple scattering, order > 2) and
+       delta_irradiance; writes delta_density.
+     ATMO_PASS_INDIRECT_IRRADIANCE  ComputeIndirectIrradianceTexture
+       (:1573-1586) from the scattering of order `order` >= 1 (1: delta_rayleigh
+       and delta_mie with their phase functions; > 1: delta_rayleigh); writes
+       delta_irradiance and adds it to irradiance.
+     ATMO_PASS_MULTIPLE_SCATTERING  ComputeMultipleScatteringTexture
+       (:1369-1383) of order `order` >= 2: reads delta_density; writes
+       delta_rayleigh (delta multiple scattering) and adds it / the Rayleigh
+       phase function to scattering (combined layout).
+   The set-up tables and ground transmittances come from `atmosphere`, the
+   shape and `transmittance`.  Allocates its tables with cudaMallocAsync;
+   returns after the pass completed. */
+typedef enum {
+  ATMO_PASS_SCATTERING_DENSITY = 4,
+  ATMO_PASS_INDIRECT_IRRADIANCE = 5,
+  ATMO_PASS_MULTIPLE_SCATTERING = 6
+} atmo_pass_kind;
+typedef struct {
+  const float* transmittance;   /* W_T x H_T */
+  float* delta_rayleigh;        /* scattering-LUT layout */
+  float* delta_mie;             /* scattering-LUT layout (order-2 density, order-1 indirect) */
+  float* delta_irradiance;      /* W_I x H_I */
+  float* delta_density;         /* scattering-LUT layout */
+  float* scattering;            /* scattering-LUT layout (multiple scattering adds to it) */
+  float* irradiance;            /* W_I x H_I (indirect irradiance adds to it) */
+} atmo_pass_buffers;
+atmo_status atmo_run_pass(const atmo_atmosphere* atmosphere, const atmo_lut_shape* shape,
+                          atmo_pass_kind pass, unsigned order, atmo_path path,
+                          const atmo_pass_buffers* buffers, atmo_stream stream);
 
 /* ---- batched precomputation (many atmospheres, uneven shapes/orders) ------- */
 /* Creates a batch of n independent atmospheres, each with its own shape and
@@ -370,13 +416,23 @@ typedef struct {
   int combined;                      /* combine_scattering_textures of every set */
   unsigned admit_window_us;          /* batching window: a queued rebuild waits up to this
                                         long for others to be admitted with it (0: none) */
+  size_t pool_max_bytes;             /* cap of the private memory pool the sets come from
+                                        (0: the device's default); a rebuild admitted under
+                                        the budget that the pool cannot serve fails with
+                                        ATMO_OOM */
 } atmo_server_config;
 typedef struct {
-  int state;             /* 0 queued, 1 running, 2 done, 3 failed */
-  atmo_status status;    /* of a failed request (ATMO_BUDGET, ATMO_NOT_READY ...) */
-  double queue_ms;       /* submission to admission / launch (-1 while queued) */
+  int state;             /* 0 queued, 1 running, 2 done, 3 failed (or cancelled) */
+  atmo_status status;    /* of a failed request (ATMO_BUDGET, ATMO_OOM, ATMO_CANCELLED ...) */
+  double queue_ms;       /* submission to admission (rebuild: budget, instance rows, batching
+                            window) or to launch (shading); -1 before */
   double latency_ms;     /* submission to completion on the GPU (-1 before) */
   uint64_t set_id;       /* the LUT set (a rebuild's own ticket) */
+  double launch_ms;      /* submission to the enqueue of its first kernel (-1 before) */
+  double device_ms;      /* GPU time (CUDA events) of the launches it took part in: the
+                            rounds of a rebuild (shared with the rebuilds batched with it),
+                            the kernel of a shading request; summed as they retire */
+  unsigned rounds;       /* those launches retired so far */
 } atmo_ticket_info;
 typedef struct {
   size_t used_bytes, budget_bytes;
@@ -402,6 +458,14 @@ atmo_status atmo_server_poll(atmo_server* server, uint64_t ticket, atmo_ticket_i
    when it failed, ATMO_TIMEOUT after timeout_ms. */
 atmo_status atmo_server_wait(atmo_server* server, uint64_t ticket, unsigned timeout_ms,
                              atmo_ticket_info* info);
+/* Cancels a request that has not completed.  A queued rebuild or shading
+   request is dropped; a rebuild already being built gets no further pass and
+   its memory returns to the budget (the blocks are freed behind the passes
+   already enqueued).  The ticket then reports state 3 with ATMO_CANCELLED;
+   shading requests waiting on a cancelled set fail with ATMO_NOT_READY.  A
+   launched shading request, or a rebuild whose last pass is enqueued, cannot
+   be cancelled (ATMO_INVALID_ARG). */
+atmo_status atmo_server_cancel(atmo_server* server, uint64_t ticket);
 /* Forgets a completed shading ticket (rebuild tickets go with their set). */
 atmo_status atmo_server_release_ticket(atmo_server* server, uint64_t ticket);
 /* The render-time query interface of a ready set (marks it used). */

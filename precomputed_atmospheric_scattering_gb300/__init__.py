@@ -26,7 +26,7 @@ kLambdaR = 680.0
 kLambdaG = 550.0
 kLambdaB = 440.0
 
-OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, BUDGET, UNAVAILABLE, NOT_READY = range(8)
+OK, INVALID_ARG, OOM, CUDA_ERROR, TIMEOUT, BUDGET, UNAVAILABLE, NOT_READY, CANCELLED = range(9)
 LUT_TRANSMITTANCE, LUT_SCATTERING, LUT_SINGLE_MIE, LUT_IRRADIANCE = range(4)
 PATH_FAST, PATH_PLAIN = 0, 1
 
@@ -141,12 +141,13 @@ class Tuning(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_rebuilds_in_flight", C.c_uint),
                 ("shade_streams", C.c_uint), ("combined", C.c_int),
-                ("admit_window_us", C.c_uint)]
+                ("admit_window_us", C.c_uint), ("pool_max_bytes", C.c_size_t)]
 
 
 class TicketInfo(C.Structure):
     _fields_ = [("state", C.c_int), ("status", C.c_int), ("queue_ms", C.c_double),
-                ("latency_ms", C.c_double), ("set_id", C.c_uint64)]
+                ("latency_ms", C.c_double), ("set_id", C.c_uint64), ("launch_ms", C.c_double),
+                ("device_ms", C.c_double), ("rounds", C.c_uint)]
 
 
 class ServerStats(C.Structure):
@@ -154,6 +155,13 @@ class ServerStats(C.Structure):
                 ("resident_sets", C.c_uint), ("building", C.c_uint), ("pending", C.c_uint),
                 ("evictions", C.c_ulonglong), ("rounds", C.c_ulonglong),
                 ("kernels", C.c_ulonglong), ("shades_launched", C.c_ulonglong)]
+
+
+class PassBuffers(C.Structure):
+    """atmo_pass_buffers: device pointers (ints) of one atmo_run_pass."""
+    _fields_ = [(n, C.c_void_p) for n in ("transmittance", "delta_rayleigh", "delta_mie",
+                                           "delta_irradiance", "delta_density", "scattering",
+                                           "irradiance")]
 
 
 class LutView(C.Structure):
@@ -206,6 +214,8 @@ def lib():
                                 C.c_int, C.c_int, vp, vp, vp, vp, vp],
             "atmo_precompute_noalloc": [P(Atmosphere), P(LutShape), C.c_uint, P(C.c_float),
                                         C.c_int, C.c_int, vp, vp, vp, vp, vp],
+            "atmo_run_pass": [P(Atmosphere), P(LutShape), C.c_int, C.c_uint, C.c_int,
+                              P(PassBuffers), vp],
             "atmo_batch_create": [P(Atmosphere), P(LutShape), P(C.c_uint), C.c_uint, C.c_int,
                                   P(vp)],
             "atmo_batch_destroy": [vp],
@@ -237,6 +247,7 @@ def lib():
             "atmo_server_poll": [vp, C.c_uint64, P(TicketInfo)],
             "atmo_server_wait": [vp, C.c_uint64, C.c_uint, P(TicketInfo)],
             "atmo_server_release_ticket": [vp, C.c_uint64],
+            "atmo_server_cancel": [vp, C.c_uint64],
             "atmo_server_lut_set": [vp, C.c_uint64, P(vp)],
             "atmo_server_evict": [vp, C.c_uint64],
             "atmo_server_get_stats": [vp, P(ServerStats)],
@@ -251,7 +262,7 @@ def lib():
             f = getattr(L, name)
             f.restype = st
             f.argtypes = args
-        if L.atmo_abi_version() != 2:
+        if L.atmo_abi_version() != 3:
             raise ImportError("libatmo_gb300.so ABI version mismatch")
         _lib = L
     return _lib
@@ -554,9 +565,9 @@ class Server:
     QUEUED, RUNNING, DONE, FAILED = range(4)
 
     def __init__(self, hbm_budget_bytes=0, max_rebuilds_in_flight=0, shade_streams=0,
-                 combined=True, admit_window_us=0):
+                 combined=True, admit_window_us=0, pool_max_bytes=0):
         cfg = ServerConfig(hbm_budget_bytes, max_rebuilds_in_flight, shade_streams,
-                           int(bool(combined)), admit_window_us)
+                           int(bool(combined)), admit_window_us, pool_max_bytes)
         h = C.c_void_p()
         _check(lib().atmo_server_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -596,6 +607,11 @@ class Server:
         info = TicketInfo()
         _check(lib().atmo_server_wait(self._h, ticket, timeout_ms, C.byref(info)))
         return info
+
+    def cancel(self, ticket):
+        """Drops a queued request, or stops a rebuild being built (its memory
+        returns to the budget); the ticket then fails with CANCELLED."""
+        _check(lib().atmo_server_cancel(self._h, ticket))
 
     def release_ticket(self, ticket):
         _check(lib().atmo_server_release_ticket(self._h, ticket))
@@ -727,6 +743,25 @@ class Batch:
         _check(lib().atmo_batch_read_lut(self._h, i, kind,
                                          out.ctypes.data_as(C.POINTER(C.c_float)), out.nbytes))
         return out if v.depth > 1 else out[0]
+
+
+PASS_SCATTERING_DENSITY, PASS_INDIRECT_IRRADIANCE, PASS_MULTIPLE_SCATTERING = 4, 5, 6
+
+
+def run_pass(atmosphere, shape, pass_kind, order, path=PATH_FAST, stream=None, **buffers):
+    """One pass of Model::Precompute's order loop (atmosphere/model.cc:1137-1211)
+    on caller-owned float32 RGBA device LUTs (keyword arguments named as the
+    fields of atmo_pass_buffers: CUDA tensors or device pointers; the pass
+    reads and writes them as atmo_run_pass documents).  Synchronous."""
+    a = Atmosphere.from_buffer_of(atmosphere)
+    s = LutShape.of(shape) or LutShape(*DEFAULT_SHAPE)
+    ptr = lambda t: None if t is None else (t if isinstance(t, int) else t.data_ptr())  # noqa
+    unknown = set(buffers) - {n for n, _ in PassBuffers._fields_}
+    if unknown:
+        raise TypeError("unknown buffers: %s" % sorted(unknown))
+    b = PassBuffers(*[ptr(buffers.get(n)) for n, _ in PassBuffers._fields_])
+    _check(lib().atmo_run_pass(C.byref(a), C.byref(s), pass_kind, order, path, C.byref(b),
+                               _stream_ptr(stream)))
 
 
 def precompute(atmosphere, shape, num_scattering_orders, transmittance, scattering, single_mie,

@@ -25,6 +25,13 @@
 // Completion.  A host function enqueued behind an instance's last pass (or a
 // shading kernel) stamps its ticket; latencies are measured on the host
 // clock from submission to that stamp.  Every wait of the API is bounded.
+// Each round (and each shading launch) is bracketed by timing events, so a
+// ticket also reports the GPU time of the launches it took part in.
+//
+// Cancellation.  A queued request is dropped; a rebuild being built stops
+// after the passes already enqueued: its memory goes back to the pool behind
+// them (stream-ordered frees) and its instance row once the GPU has passed
+// them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -94,9 +101,13 @@ struct Ticket {
   enum State { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3 };
   std::atomic<int> state{kQueued};
   atmo_status status = ATMO_OK;
-  Clock::time_point submitted, started, finished;
+  Clock::time_point submitted, started, launched, finished;
   bool is_rebuild = false;
+  bool has_launched = false;   // its first kernel has been enqueued
+  double device_ms = 0.0;      // GPU time of the retired launches it took part in
+  unsigned rounds = 0;         // those launches (rounds, or the shading kernel)
   uint64_t set_id = 0;
+  std::string message;         // why it failed
 };
 
 // A resident (or building) LUT set.
@@ -134,14 +145,18 @@ struct ShadeRequest {
 };
 
 struct Round {
+  cudaEvent_t start = nullptr;         // timing events around the round's launches
   cudaEvent_t done = nullptr;
+  std::vector<uint64_t> members;       // rebuild tickets with a pass in this round
   std::vector<uint64_t> finishing;     // sets whose last pass ran in this round
+  std::vector<int> release_rows;       // instance rows freed once the round completes
   size_t ring_offset = 0, ring_ints = 0;
 };
 
 struct ShadeInFlight {
-  cudaEvent_t done = nullptr;
+  cudaEvent_t start = nullptr, done = nullptr;
   uint64_t set_id = 0;
+  uint64_t ticket = 0;
 };
 
 void StampDone(void* p) {
@@ -200,10 +215,12 @@ struct atmo_server {
   bool RetireRounds();
   bool LaunchShades();
   bool RetireShades();
-  void FailTicket(uint64_t id, atmo_status st) {
+  atmo_status Cancel(uint64_t id);
+  void FailTicket(uint64_t id, atmo_status st, const std::string& why) {
     auto it = tickets.find(id);
     if (it == tickets.end()) return;
     it->second->status = st;
+    it->second->message = why;
     it->second->finished = Clock::now();
     it->second->state.store(Ticket::kFailed, std::memory_order_release);
   }
@@ -228,6 +245,7 @@ atmo_status atmo_server::Init() {
   props.handleTypes = cudaMemHandleTypeNone;
   props.location.type = cudaMemLocationTypeDevice;
   props.location.id = device;
+  props.maxSize = cfg.pool_max_bytes;   // 0: the device's default
   ATMO_CUDA_TRY(cudaMemPoolCreate(&pool, &props));
   uint64_t keep = UINT64_MAX;   // keep freed blocks for reuse
   ATMO_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
@@ -252,8 +270,14 @@ void atmo_server::Shutdown() {
   cudaSetDevice(device);
   if (build_stream) cudaStreamSynchronize(build_stream);
   for (cudaStream_t st : shade_streams) cudaStreamSynchronize(st);
-  for (Round& r : rounds) cudaEventDestroy(r.done);
-  for (ShadeInFlight& s : shades) cudaEventDestroy(s.done);
+  for (Round& r : rounds) {
+    if (r.start) cudaEventDestroy(r.start);
+    cudaEventDestroy(r.done);
+  }
+  for (ShadeInFlight& s : shades) {
+    cudaEventDestroy(s.start);
+    cudaEventDestroy(s.done);
+  }
   for (auto& kv : slots) {
     if (kv.second->final_block) cudaFreeAsync(kv.second->final_block, build_stream);
     if (kv.second->scratch_block) cudaFreeAsync(kv.second->scratch_block, build_stream);
@@ -315,18 +339,23 @@ bool atmo_server::Admit(std::unique_lock<std::mutex>&) {
     RebuildRequest& rq = pending_rebuilds.front();
     const size_t fb = FinalBytes(rq.s, cfg.combined != 0), sb = ScratchBytes(rq.s);
     if (fb + sb > cfg.hbm_budget_bytes) {
-      SetError("a rebuild needs more than the whole device-memory budget");
-      FailTicket(rq.ticket, ATMO_BUDGET);
+      FailTicket(rq.ticket, ATMO_BUDGET,
+                 "a rebuild needs more than the whole device-memory budget");
       pending_rebuilds.pop_front();
       continue;
     }
     if (!EvictFor(fb + sb)) break;   // wait for sets to become idle or finish
     void* fblock = nullptr;
     void* sblock = nullptr;
-    if (cudaMallocFromPoolAsync(&fblock, fb, pool, build_stream) != cudaSuccess ||
-        cudaMallocFromPoolAsync(&sblock, sb, pool, build_stream) != cudaSuccess) {
+    cudaError_t ae = cudaMallocFromPoolAsync(&fblock, fb, pool, build_stream);
+    if (ae == cudaSuccess) ae = cudaMallocFromPoolAsync(&sblock, sb, pool, build_stream);
+    if (ae != cudaSuccess) {
+      // Not sticky: clear it, or the next launch check would report it.
+      cudaGetLastError();
       if (fblock) cudaFreeAsync(fblock, build_stream);
-      FailTicket(rq.ticket, ATMO_OOM);
+      FailTicket(rq.ticket, ae == cudaErrorMemoryAllocation ? ATMO_OOM : ATMO_CUDA_ERROR,
+                 std::string("the memory pool cannot serve the rebuild: ") +
+                     cudaGetErrorString(ae));
       pending_rebuilds.pop_front();
       continue;
     }
@@ -459,6 +488,8 @@ bool atmo_server::LaunchRound() {
     off += 2 * n + 1;
   }
   ring_head += need;
+  cudaEventCreate(&round.start);
+  cudaEventRecord(round.start, build_stream);
   cudaError_t e = cudaMemcpyAsync(d_ring + round.ring_offset, h, need * sizeof(int),
                                   cudaMemcpyHostToDevice, build_stream);
   for (const Launch& l : launches) {
@@ -468,13 +499,20 @@ bool atmo_server::LaunchRound() {
   }
   if (e != cudaSuccess) {
     worker_error = std::string("round launch: ") + cudaGetErrorString(e);
-    for (uint64_t id : building) FailTicket(id, ATMO_CUDA_ERROR);
+    for (uint64_t id : building) FailTicket(id, ATMO_CUDA_ERROR, worker_error);
     building.clear();
     return false;
   }
   // Advance; instances past their last pass complete with this round.
   std::vector<uint64_t> still;
+  const Clock::time_point now = Clock::now();
+  round.members = building;
   for (uint64_t id : building) {
+    Ticket* t = tickets[id].get();
+    if (!t->has_launched) {
+      t->has_launched = true;
+      t->launched = now;
+    }
     LutSlot* s = slots[id].get();
     if (++s->next == s->seq.size()) {
       round.finishing.push_back(id);
@@ -488,7 +526,7 @@ bool atmo_server::LaunchRound() {
     }
   }
   building.swap(still);
-  cudaEventCreateWithFlags(&round.done, cudaEventDisableTiming);
+  cudaEventCreate(&round.done);
   cudaEventRecord(round.done, build_stream);
   rounds.push_back(round);
   ++stats.rounds;
@@ -499,6 +537,19 @@ bool atmo_server::RetireRounds() {
   bool any = false;
   while (!rounds.empty() && cudaEventQuery(rounds.front().done) == cudaSuccess) {
     Round& r = rounds.front();
+    if (r.start) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, r.start, r.done) == cudaSuccess) {
+        for (uint64_t id : r.members) {
+          auto ti = tickets.find(id);
+          if (ti == tickets.end()) continue;
+          ti->second->device_ms += ms;
+          ++ti->second->rounds;
+        }
+      }
+      cudaEventDestroy(r.start);
+    }
+    for (int row : r.release_rows) free_rows.push_back(row);
     for (uint64_t id : r.finishing) {
       auto it = slots.find(id);
       if (it == slots.end()) continue;
@@ -526,8 +577,7 @@ bool atmo_server::LaunchShades() {
         ++it;
         continue;
       }
-      SetError("LUT set evicted or unknown");
-      FailTicket(it->ticket, ATMO_NOT_READY);
+      FailTicket(it->ticket, ATMO_NOT_READY, "LUT set evicted, cancelled or unknown");
       it = pending_shades.erase(it);
       continue;
     }
@@ -554,18 +604,23 @@ bool atmo_server::LaunchShades() {
     v.sky = reinterpret_cast<float4*>(it->sky);
     v.shaded = reinterpret_cast<float4*>(it->shaded);
     Ticket* t = tickets[it->ticket].get();
-    t->started = Clock::now();
+    t->started = t->launched = Clock::now();
+    t->has_launched = true;
     t->state.store(Ticket::kRunning, std::memory_order_release);
+    ShadeInFlight f;
+    cudaEventCreate(&f.start);
+    cudaEventRecord(f.start, st);
     cudaError_t e = LaunchShadeView(s->view.luts, v, st);
     if (e != cudaSuccess) {
-      SetError(std::string("shading launch: ") + cudaGetErrorString(e));
-      FailTicket(it->ticket, ATMO_CUDA_ERROR);
+      FailTicket(it->ticket, ATMO_CUDA_ERROR,
+                 std::string("shading launch: ") + cudaGetErrorString(e));
+      cudaEventDestroy(f.start);
     } else {
-      cudaLaunchHostFunc(st, StampDone, t);
-      ShadeInFlight f;
-      cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
+      cudaEventCreate(&f.done);
       cudaEventRecord(f.done, st);
+      cudaLaunchHostFunc(st, StampDone, t);
       f.set_id = s->id;
+      f.ticket = it->ticket;
       ++s->pins;
       s->last_use = ++lru_clock;
       shades.push_back(f);
@@ -586,11 +641,75 @@ bool atmo_server::RetireShades() {
     }
     auto si = slots.find(it->set_id);
     if (si != slots.end()) --si->second->pins;
+    float ms = 0.0f;
+    auto ti = tickets.find(it->ticket);
+    if (ti != tickets.end() && cudaEventElapsedTime(&ms, it->start, it->done) == cudaSuccess) {
+      ti->second->device_ms += ms;
+      ++ti->second->rounds;
+    }
+    cudaEventDestroy(it->start);
     cudaEventDestroy(it->done);
     it = shades.erase(it);
     any = true;
   }
   return any;
+}
+
+// Cancels ticket `id` (the lock is held).  A queued request is dropped.  A
+// rebuild being built gets no further pass: its blocks are freed behind the
+// passes already enqueued on the build stream (stream-ordered), its budget
+// is released now, and its instance row once the GPU has passed the event
+// recorded here (the rounds in flight still read the row).
+atmo_status atmo_server::Cancel(uint64_t id) {
+  auto ti = tickets.find(id);
+  if (ti == tickets.end()) {
+    SetError("unknown ticket");
+    return ATMO_INVALID_ARG;
+  }
+  Ticket* t = ti->second.get();
+  if (t->state.load() >= Ticket::kDone) {
+    SetError("ticket already complete");
+    return ATMO_INVALID_ARG;
+  }
+  if (!t->is_rebuild) {
+    for (auto it = pending_shades.begin(); it != pending_shades.end(); ++it) {
+      if (it->ticket != id) continue;
+      pending_shades.erase(it);
+      FailTicket(id, ATMO_CANCELLED, "cancelled");
+      return ATMO_OK;
+    }
+    SetError("shading request already launched");
+    return ATMO_INVALID_ARG;
+  }
+  for (auto it = pending_rebuilds.begin(); it != pending_rebuilds.end(); ++it) {
+    if (it->ticket != id) continue;
+    pending_rebuilds.erase(it);
+    FailTicket(id, ATMO_CANCELLED, "cancelled");
+    return ATMO_OK;
+  }
+  auto bi = std::find(building.begin(), building.end(), id);
+  auto si = slots.find(id);
+  if (bi == building.end() || si == slots.end()) {
+    SetError("rebuild already complete on the GPU");
+    return ATMO_INVALID_ARG;
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device);
+  building.erase(bi);
+  LutSlot* slot = si->second.get();
+  const int row = slot->index;
+  slot->index = -1;   // FreeSlot must not return the row yet
+  FreeSlot(slot);
+  Round release;
+  release.release_rows.push_back(row);
+  cudaEventCreateWithFlags(&release.done, cudaEventDisableTiming);
+  cudaEventRecord(release.done, build_stream);
+  rounds.push_back(release);
+  slots.erase(si);
+  FailTicket(id, ATMO_CANCELLED, "cancelled");
+  cudaSetDevice(prev);
+  return ATMO_OK;
 }
 
 void atmo_server::WorkerLoop() {
@@ -705,11 +824,13 @@ atmo_status atmo_server_submit_shade(atmo_server* s, uint64_t set_id,
 static void FillInfo(const Ticket& t, atmo_ticket_info* info) {
   info->state = t.state.load(std::memory_order_acquire);
   info->status = t.status;
-  info->queue_ms = info->state >= Ticket::kRunning || info->state == Ticket::kFailed
-                       ? MsSince(t.submitted, t.started)
-                       : -1.0;
+  const bool started = t.started != Clock::time_point{};   // admitted or launched
+  info->queue_ms = started ? MsSince(t.submitted, t.started) : -1.0;
   info->latency_ms = info->state >= Ticket::kDone ? MsSince(t.submitted, t.finished) : -1.0;
   info->set_id = t.set_id;
+  info->launch_ms = t.has_launched ? MsSince(t.submitted, t.launched) : -1.0;
+  info->device_ms = t.device_ms;
+  info->rounds = t.rounds;
 }
 
 atmo_status atmo_server_poll(atmo_server* s, uint64_t ticket, atmo_ticket_info* info) {
@@ -732,7 +853,7 @@ atmo_status atmo_server_wait(atmo_server* s, uint64_t ticket, unsigned timeout_m
       if (it == s->tickets.end()) return Fail(ATMO_INVALID_ARG, "unknown ticket");
       FillInfo(*it->second, info);
       if (info->state >= Ticket::kDone) {
-        if (info->state == Ticket::kFailed) return info->status;
+        if (info->state == Ticket::kFailed) return Fail(info->status, it->second->message);
         // A rebuild's set is usable once its round has been retired.
         if (it->second->is_rebuild) {
           auto si = s->slots.find(ticket);
@@ -746,6 +867,17 @@ atmo_status atmo_server_wait(atmo_server* s, uint64_t ticket, unsigned timeout_m
     if (Clock::now() >= deadline) return Fail(ATMO_TIMEOUT, "ticket not complete");
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+}
+
+atmo_status atmo_server_cancel(atmo_server* s, uint64_t ticket) {
+  if (!s) return Fail(ATMO_INVALID_ARG, "NULL server");
+  atmo_status st;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    st = s->Cancel(ticket);
+  }
+  s->cv.notify_all();
+  return st;
 }
 
 atmo_status atmo_server_release_ticket(atmo_server* s, uint64_t ticket) {

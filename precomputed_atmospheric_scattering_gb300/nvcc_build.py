@@ -26,7 +26,7 @@ UNIT_FLAGS = {"atmo_tables.cu": ["--fmad=false"],
               "atmo_rays.cu": ["--prec-div=false", "--prec-sqrt=false"],
               "atmo_fast.cu": ["--prec-div=false", "--prec-sqrt=false"]}
 UNITS = ["atmo_tables.cu", "atmo_kernels.cu", "atmo_rays.cu", "atmo_fast.cu", "atmo_program.cu", "atmo_render.cu", "atmo_server.cu",
-         "atmo_capi.cu", "atmo_noalloc.cu"]
+         "atmo_capi.cu", "atmo_noalloc.cu", "atmo_pass_api.cu"]
 
 
 def nvcc():

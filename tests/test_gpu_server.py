@@ -4,6 +4,7 @@ sets resident under an HBM budget with LRU eviction.  Each result must be the
 same alone and in the mix (bit for bit: the kernels assign tiles per
 instance), and the same as the standalone batched precomputation."""
 import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -185,3 +186,106 @@ def test_destroy_with_work_in_flight(atmo, oracle, torch_cuda):
     srv.close()
     assert time.perf_counter() - t0 < 60.0
     torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
+def test_pool_that_cannot_serve_an_admitted_rebuild_fails_it_with_oom(atmo, oracle, torch_cuda):
+    """The budget admits the rebuild but the private pool, capped below one
+    set, cannot serve it: the ticket fails with ATMO_OOM (the allocation
+    failure branch of admission), and the server goes on serving requests
+    that fit."""
+    srv = atmo.Server(pool_max_bytes=32 << 20)
+    try:
+        t = srv.submit_rebuild(oracle.earth_atmosphere(), atmo.DEFAULT_SHAPE, 4)  # ~65 MB
+        with pytest.raises(atmo.AtmoError) as e:
+            srv.wait(t, 60000)
+        assert e.value.status == atmo.OOM
+        info = srv.poll(t)
+        assert info.state == atmo.Server.FAILED and info.status == atmo.OOM
+        small = srv.submit_rebuild(oracle.earth_atmosphere(), SMALL, 2)            # ~0.3 MB
+        assert srv.wait(small, 60000).state == atmo.Server.DONE
+        assert srv.stats().used_bytes > 0
+    finally:
+        srv.close()
+
+
+@pytest.mark.gpu
+def test_wait_times_out_on_a_ticket_held_by_the_batching_window(atmo, oracle, torch_cuda):
+    """A lone rebuild waits for company for the batching window (2 s): a wait
+    of 50 ms on it returns ATMO_TIMEOUT with the ticket still queued; a
+    longer wait then sees it complete."""
+    srv = atmo.Server(admit_window_us=2000000)
+    try:
+        t = srv.submit_rebuild(oracle.earth_atmosphere(), SMALL, 2)
+        with pytest.raises(atmo.AtmoError) as e:
+            srv.wait(t, 50)
+        assert e.value.status == atmo.TIMEOUT
+        assert srv.poll(t).state == atmo.Server.QUEUED
+        info = srv.wait(t, 60000)
+        assert info.state == atmo.Server.DONE
+        assert info.queue_ms >= 1900.0            # held by the window
+        assert info.rounds == 7 and info.device_ms > 0.0   # 4 + 3 passes, GPU-timed
+    finally:
+        srv.close()
+
+
+@pytest.mark.gpu
+def test_cancel_a_queued_rebuild_and_its_shading(atmo, oracle, torch_cuda):
+    """A rebuild held by the batching window is dropped by cancel; a shading
+    request waiting on its set then fails with ATMO_NOT_READY, and a shading
+    request still queued can be cancelled itself."""
+    torch = torch_cuda
+    srv = atmo.Server(admit_window_us=5000000)
+    try:
+        c = srv.submit_rebuild(oracle.earth_atmosphere(), SMALL, 2)
+        view, depth = make_view(atmo, 3)
+        s1, keep1 = shade(torch, srv, c, view, depth)
+        s2, keep2 = shade(torch, srv, c, view, depth)
+        assert srv.poll(c).state == atmo.Server.QUEUED
+        srv.cancel(s2)
+        srv.cancel(c)
+        for t, status in ((c, atmo.CANCELLED), (s2, atmo.CANCELLED), (s1, atmo.NOT_READY)):
+            with pytest.raises(atmo.AtmoError) as e:
+                srv.wait(t, 10000)
+            assert e.value.status == status
+        assert srv.stats().used_bytes == 0 and srv.stats().pending == 0
+    finally:
+        srv.close()
+
+
+@pytest.mark.gpu
+def test_cancel_a_running_rebuild_releases_its_budget(atmo, oracle, torch_cuda):
+    """Cancelling a rebuild being built stops it after the passes already
+    enqueued and returns its memory to the budget, so a rebuild that did not
+    fit beside it is admitted and built; completed tickets cannot be
+    cancelled."""
+    torch = torch_cuda
+    one_set = 70 << 20     # one default-shape set (~65 MB while building) fits, two do not
+    srv = atmo.Server(hbm_budget_bytes=one_set)
+    try:
+        # a: 64 orders (193 passes, tens of ms); b waits for the budget a holds.
+        a = srv.submit_rebuild(oracle.earth_atmosphere(), atmo.DEFAULT_SHAPE, 64)
+        deadline = time.monotonic() + 10.0
+        while srv.poll(a).state == atmo.Server.QUEUED and time.monotonic() < deadline:
+            time.sleep(0.0005)
+        b = srv.submit_rebuild(oracle.earth_atmosphere(mie_g=0.7), atmo.DEFAULT_SHAPE, 4)
+        view, depth = make_view(atmo, 4)
+        s_b, keep = shade(torch, srv, b, view, depth)
+        assert srv.poll(a).state == atmo.Server.RUNNING
+        time.sleep(0.002)
+        assert srv.poll(b).state == atmo.Server.QUEUED
+        srv.cancel(a)
+        with pytest.raises(atmo.AtmoError) as e:
+            srv.wait(a, 1000)
+        assert e.value.status == atmo.CANCELLED
+        # Its budget went back: b is admitted and built, and its shading runs.
+        assert srv.wait(b, 60000).state == atmo.Server.DONE
+        assert srv.wait(s_b, 60000).state == atmo.Server.DONE
+        with pytest.raises(atmo.AtmoError) as e:
+            srv.cancel(b)
+        assert e.value.status == atmo.INVALID_ARG
+        torch.cuda.synchronize()
+        st = srv.stats()
+        assert st.building == 0 and 0 < st.used_bytes <= one_set
+    finally:
+        srv.close()
