@@ -20,10 +20,22 @@
 // temporary is written in full by an earlier pass of the same call before any
 // pass reads it.
 //
+// The array's memory is taken when this file's device code is loaded: with
+// CUDA's default lazy module loading, by the first call on each device (the
+// one that looks up the array's address), or at context creation with
+// CUDA_MODULE_LOADING=EAGER.  A host application that reserves all device
+// memory up front should make one call (or load eagerly) before reserving.
+//
 // Host code cannot use the array's symbol as a device address (it names a
-// host-side stand-in); the device address is obtained once per device with
-// cudaGetSymbolAddress on the first call made with that device current, so
-// that first call should come before any stream capture.
+// host-side stand-in); the device address comes from cudaGetSymbolAddress,
+// looked up on the first call made in each CUDA context (a context that is
+// destroyed and re-created, e.g. by cudaDeviceReset, gets a fresh lookup), so
+// that first call should come before any stream capture.  The launch
+// descriptors (the instance record and the per-pass work lists) reach the
+// scratch array as by-value kernel parameters of a set-up kernel: a call
+// copies nothing from host memory and does not wait for earlier work in the
+// stream.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -44,8 +56,97 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 namespace {
 
 constexpr int kMaxDevices = 64;
+constexpr int kMaxOrders = 64;
+constexpr int kMaxSteps = 4 + 3 * (kMaxOrders - 1);
+
+// The launch descriptors of one call, passed by value to the set-up kernel.
+struct NoAllocDescriptors {
+  Instance in;
+  int steps;
+  int tiles[kMaxSteps];
+};
+
+// Writes the instance record and the work lists {inst = 0; start = 0,
+// tiles} of every step into the scratch array.
+__global__ void k_noalloc_setup(const NoAllocDescriptors d, Instance* in_dst, int* wl_dst) {
+  const int* src = reinterpret_cast<const int*>(&d.in);
+  int* dst = reinterpret_cast<int*>(in_dst);
+  constexpr int kWords = (int)(sizeof(Instance) / sizeof(int));
+  for (int i = threadIdx.x; i < kWords; i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < d.steps; i += blockDim.x) {
+    wl_dst[3 * i] = 0;
+    wl_dst[3 * i + 1] = 0;
+    wl_dst[3 * i + 2] = d.tiles[i];
+  }
+}
+static_assert(sizeof(Instance) % sizeof(int) == 0, "the set-up kernel copies whole words");
+static_assert(sizeof(NoAllocDescriptors) <= 4000, "the descriptors must fit a kernel's parameters");
+
+// Per device: the CUDA context (its process-unique id) in which the scratch
+// array's address was looked up, and that address.
+struct ScratchAddress {
+  unsigned long long ctx_id = 0;
+  void* ptr = nullptr;
+};
 std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+ScratchAddress g_noalloc_addr[kMaxDevices];
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// The process-unique id of the calling thread's current context, or 0 when
+// none is current (the driver entry points come through the runtime, so the
+// library does not link libcuda).
+unsigned long long CurrentContextId() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(fn);
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// The scratch array's device address in the current context of device
+// `dev`: looked up on the first call in each context.
+atmo_status ScratchBase(int dev, unsigned char** base) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  ScratchAddress& a = g_noalloc_addr[dev];
+  const unsigned long long ctx = CurrentContextId();
+  if (a.ptr && ctx != 0 && ctx == a.ctx_id) {
+    *base = static_cast<unsigned char*>(a.ptr);
+    return ATMO_OK;
+  }
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    SetError("atmo_precompute_noalloc: loading its 64 MiB scratch array failed for lack of "
+             "device memory; make one call (or set CUDA_MODULE_LOADING=EAGER) before "
+             "reserving the device's memory");
+    return ATMO_OOM;
+  }
+  if (e != cudaSuccess) return CudaFail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+  a.ptr = p;
+  a.ctx_id = CurrentContextId();   // the lookup made the context current if none was
+  *base = static_cast<unsigned char*>(p);
+  return ATMO_OK;
+}
 
 size_t Align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -99,7 +200,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     SetError("single_mie is required when combined == 0");
     return ATMO_INVALID_ARG;
   }
-  if (num_scattering_orders < 1 || num_scattering_orders > 64) {
+  if (num_scattering_orders < 1 || num_scattering_orders > (unsigned)kMaxOrders) {
     SetError("num_scattering_orders must be in [1, 64]");
     return ATMO_INVALID_ARG;
   }
@@ -134,13 +235,7 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     add(Pass::kIndirect, (int)order - 1);
     add(Pass::kMultiple, (int)order);
   }
-  std::vector<int> wl_ints;
-  for (const PlannedStep& p : steps) {
-    wl_ints.push_back(0);          // inst[0]
-    wl_ints.push_back(0);          // start[0]
-    wl_ints.push_back(p.tiles);    // start[1]
-  }
-  const NoAllocLayout L = Layout(s, wl_ints.size());
+  const NoAllocLayout L = Layout(s, 3 * steps.size());
   if (L.total > kNoAllocScratchBytes) {
     SetError("atmo_precompute_noalloc: this LUT shape needs " + std::to_string(L.total) +
              " bytes of temporaries, more than the fixed " +
@@ -148,8 +243,6 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     return ATMO_BUDGET;
   }
 
-  // Device address of the scratch array on the current device (set-up on the
-  // first call per device).
   int dev = 0;
   ATMO_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) {
@@ -157,19 +250,12 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
     return ATMO_INVALID_ARG;
   }
   unsigned char* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess) return CudaFail(e, "cudaGetSymbolAddress(no-alloc scratch)");
-      g_noalloc_ptr[dev] = p;
-    }
-    base = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
-  }
+  const atmo_status found = ScratchBase(dev, &base);
+  if (found != ATMO_OK) return found;
 
-  Instance in;
-  std::memset(&in, 0, sizeof(in));
+  NoAllocDescriptors d;
+  std::memset(&d, 0, sizeof(d));
+  Instance& in = d.in;
   in.c = consts;
   in.s = s;
   in.T = reinterpret_cast<float4*>(transmittance);
@@ -188,22 +274,22 @@ extern "C" atmo_status atmo_precompute_noalloc(const atmo_atmosphere* atmosphere
   in.tab.drows = reinterpret_cast<DensityRow*>(base + L.drows);
   in.tab.irows = reinterpret_cast<IrrRow*>(base + L.irows);
   in.tab.mus_i = reinterpret_cast<float*>(base + L.mus_i);
+  d.steps = (int)steps.size();
+  for (size_t i = 0; i < steps.size(); ++i) d.tiles[i] = steps[i].tiles;
 
-  // Launch descriptors into the scratch array (pageable copies: the host
-  // buffers may be released once the calls return).
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  ATMO_CUDA_TRY(cudaMemcpyAsync(base + L.instance, &in, sizeof(in), cudaMemcpyHostToDevice, st));
-  ATMO_CUDA_TRY(cudaMemcpyAsync(base + L.worklists, wl_ints.data(), wl_ints.size() * sizeof(int),
-                                cudaMemcpyHostToDevice, st));
-  const Instance* d_in = reinterpret_cast<const Instance*>(base + L.instance);
-  const int* d_wl = reinterpret_cast<const int*>(base + L.worklists);
+  Instance* d_in = reinterpret_cast<Instance*>(base + L.instance);
+  int* d_wl = reinterpret_cast<int*>(base + L.worklists);
+  k_noalloc_setup<<<1, 256, 0, st>>>(d, d_in, d_wl);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return CudaFail(e, "no-alloc set-up launch");
   for (size_t i = 0; i < steps.size(); ++i) {
     WorkList wl;
     wl.inst = d_wl + 3 * i;
     wl.start = d_wl + 3 * i + 1;
     wl.count = 1;
-    cudaError_t e = LaunchPass(steps[i].pass, steps[i].order, steps[i].smem, d_in, wl,
-                               steps[i].tiles, steps[i].path, st);
+    e = LaunchPass(steps[i].pass, steps[i].order, steps[i].smem, d_in, wl, steps[i].tiles,
+                   steps[i].path, st);
     if (e != cudaSuccess) return CudaFail(e, "kernel launch");
   }
   return ATMO_OK;
