@@ -5,36 +5,45 @@ reference's default LUT shape (transmittance 256x64, scattering NU 8 x MU_S 32
 x MU 128 x R 32 = 256x128x32 RGBA, irradiance 64x16), 4 scattering orders,
 3 wavelengths (680/550/440 nm), combined scattering textures, FP32 -- the
 Earth parameters of atmosphere/demo/demo.cc:188-284 with max sun zenith 102
-degrees.  Every instance's working set (64 MB) exceeds nothing in L2 on its
-own, and a batch of B >= 4 is several times larger than the 129 MB L2, so no
-explicit L2 flush is needed between steps.
+degrees.  A batch of B >= 4 (64 MB of LUTs and temporaries per instance) is
+several times larger than the 129 MB L2, so no explicit L2 flush is needed
+between steps.
 
-Reported (one JSON line on rank 0):
+Rank 0 prints one compact JSON line (the headline figures); the full record
+(per-pass times, parity, the mixed batch, serving, the other configurations)
+goes to stderr as one line starting with "detail: " and, when ATMO_BENCH_OUT
+names a directory, to bench_detail.json there.  Reported:
   value          batched rebuilds/s (device-timed with CUDA events),
   e2e            the same through the public C API with host buffers: every
                  step's atmosphere parameters go host->device and all its LUTs
                  come back device->host into pinned memory inside the timed
                  region (two batches alternate, so a step's read-back overlaps
                  the next step's rebuilds),
-  single_rebuild p50/p99 latency of one Model.Init (fast path) and the plain
-                 path's rebuilds/s,
-  roofline       the scattering-density kernel against this GPU's FP32 FMA
-                 throughput measured in the same run: the reference
-                 algorithm's FLOPs per direction sample (counted in the
-                 oracle, tests/golden/flops_config0.json) over the launch
-                 time, and the FLOPs the kernel executes (ncu),
+  the benchmark spec     single-rebuild p50 latency (fast path), the plain per-texel
+                 kernels' rebuilds/s and the batched / plain ratio,
+  roofline       the scattering-density kernel (the dominant one) against this
+                 GPU's FP32 FMA throughput measured in the same run: the FP32
+                 operations the kernel executes per direction sample (ncu SASS
+                 op counters) x samples / launch time; the reference
+                 algorithm's operation count (tests/golden/flops_config0.json)
+                 over the same time is reported apart, as algorithmic_rate,
   parity         per-LUT max / p99 relative error of the benchmarked LUTs at
                  the FP64 reference's committed sampled texels,
+  configs        the spectral-precision (15 wavelengths, FP16 LUTs) and the
+                 high-resolution (8 orders) rebuilds: device-timed ms and
+                 error against the FP64 GPU oracle's committed sampled texels,
   batched_mixed  256 seeded planets of uneven LUT shapes ({half, default,
                  double-R}) and 2-6 orders in one batched pass sequence,
   serving        a short seeded Poisson stream (2000 req/s, 10% rebuilds of
                  such planets, 90% shading of 1920x1080 pinhole views with the
                  three render functions) through atmo_server: p50/p99 latency
-                 per request type and throughput,
-  cpu_baseline   the FP64 CPU oracle on a bounded sample, all host threads.
+                 per request type, split into queue and run time,
+  cpu_baseline   one whole, unsampled rebuild by the FP64 CPU oracle (the
+                 reference's CPU algorithm restated), all host threads.
 
 --impl reference times the reference's CPU algorithm (the oracle port of
-atmosphere/reference/model.cc + functions.glsl) on the host cores instead.
+atmosphere/reference/model.cc + functions.glsl) on the host cores instead:
+every warm-up and timed step is one whole, unsampled rebuild.
 """
 from __future__ import annotations
 
@@ -58,11 +67,24 @@ UNIT = "rebuilds/s"
 WORKLOAD = ("Earth atmosphere LUT rebuild, 256x64 / 256x128x32 / 64x16 RGBA FP32, "
             "4 scattering orders, 3 wavelengths, combined textures")
 # FP32 operations per direction sample that the fast scattering-density kernel
-# executes (FADD + FMUL + 2 FFMA + 2 (FADD2 + FMUL2) + 4 FFMA2, counted by ncu's
-# SASS op counters over one launch: profiles/fast_kernels_earth_default_batch2.md): order 2 evaluates
-# single scattering with its phase functions, higher orders one radiance table
-# (one merged sky + ground table on the rows that hit the ground).
+# executes, from ncu's SASS op counters over one launch (an FMA counts 2, a
+# packed FP32x2 instruction 2 or 4): order 2 evaluates single scattering with
+# its phase functions, higher orders one radiance table (one merged sky +
+# ground table on the rows that hit the ground).
 DENSITY_FLOPS_PER_SAMPLE = {2: 48.9, 3: 20.1}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one density
+# launch over 16 default-shape Earth instances, from a one-pass ncu capture of
+# the batch-16 rebuild (python -m precomputed_atmospheric_scattering_gb300.
+# profile_case --batch 16): order 2 read 67.8 MB + wrote 207.4 MB, orders 3
+# and 4 read 36.0 MB + wrote 207.5 MB.
+DENSITY_DRAM_BYTES_B16 = {2: 275.27e6, 3: 243.53e6}
+# Bytes a density launch must move per default-shape Earth instance: the
+# previous order's mu rows that its 16 theta samples interpolate (484 unique
+# rows of the 4,096 per instance, 1.98 MB per species; two species at order
+# 2) and the 16.8 MB delta-density LUT it writes.  The measured bytes fall
+# below this because the last ~60 MB of writes are still dirty in the 129 MB
+# L2 when a launch ends (they are written back during the next one).
+DENSITY_COMPULSORY_BYTES = {2: 2 * 1982464 + 16777216, 3: 1982464 + 16777216}
 # The reference algorithm's operation counts of this workload, frozen from the
 # oracle's counting build (tests/golden/make_flops.py): adds and muls of the
 # shader arithmetic per direction sample of each density launch, and per
@@ -86,9 +108,17 @@ def reference_flops():
     per_sample = {l["order"]: l["flops_per_unit"] for l in d["counts"]["launches"]
                   if l["pass"] == "scattering_density"}
     return per_sample, d["counts"]["total"]["flops"]
-# DRAM bytes per density launch and instance, from the same capture
-# (dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance launch / 2).
-DENSITY_DRAM_BYTES_PER_INSTANCE = {2: 4.21e6, 3: 2.25e6}
+
+
+def rnd(x, digits=4):
+    """x rounded to `digits` significant digits (floats in nested values)."""
+    if isinstance(x, float):
+        return float("%.*g" % (digits, x)) if math.isfinite(x) else None
+    if isinstance(x, dict):
+        return {k: rnd(v, digits) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [rnd(v, digits) for v in x]
+    return x
 
 
 def parse():
@@ -134,11 +164,10 @@ def dist_info():
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (FP64 restatement of the reference CPU model).
 # ---------------------------------------------------------------------------
-def cpu_rebuild_seconds(stride=16, threads=0, by_rows=False):
-    """One rebuild by the FP64 oracle, density and multiple scattering sampled
-    on every stride-th texel and scaled.  by_rows: the threads take whole rows
-    and r-slices (the reference CPU driver's partition) instead of 64-texel
-    blocks."""
+def cpu_rebuild_seconds(threads=0, by_rows=False):
+    """(wall seconds, per-pass seconds) of one whole, unsampled rebuild by the
+    FP64 oracle.  by_rows: the threads take whole rows and r-slices (the
+    reference CPU driver's partition) instead of 64-texel blocks."""
     from oracle import oracle as O
     O.build()
     import ctypes as C
@@ -146,70 +175,61 @@ def cpu_rebuild_seconds(stride=16, threads=0, by_rows=False):
     shp = O.shape(*O.DEFAULT_SHAPE)
     sec = np.zeros(6)
     t0 = time.perf_counter()
-    rc = O.lib().oracle_time_precompute_partitioned(C.byref(atm), C.byref(shp), 4, stride,
+    rc = O.lib().oracle_time_precompute_partitioned(C.byref(atm), C.byref(shp), 4, 1,
                                                     threads, int(by_rows),
                                                     sec.ctypes.data_as(O.dp))
     wall = time.perf_counter() - t0
     if rc != 0:
         raise RuntimeError("oracle timing failed")
-    # Density and multiple scattering ran on every stride-th texel: scale them.
-    full = sec[0] + sec[1] + sec[2] + sec[4] + (sec[3] + sec[5]) * stride
-    return full, wall, sec
+    return wall, sec
 
 
-def cpu_baseline_entry(stride=16):
+def cpu_baseline_entry():
     cores = os.cpu_count() or 1
-    full, wall, sec = cpu_rebuild_seconds(stride)
-    rows_full, rows_wall, _ = cpu_rebuild_seconds(stride, by_rows=True)
-    return {"value": 1.0 / full, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": ("one config-0 Earth rebuild (4 orders) by the FP64 oracle with %d threads "
-                       "taking 64-texel blocks; transmittance, irradiance and single scattering "
-                       "in full, scattering density and multiple scattering on every %dth texel "
-                       "and scaled x%d (%.1f s of CPU wall time, extrapolated rebuild %.1f s)"
-                       % (cores, stride, stride, wall, full)),
-            "reference_partition": {
-                "value": 1.0 / rows_full, "unit": UNIT,
-                "partition": "whole texture rows and r-slices per thread, as the reference's "
-                             "CPU driver (atmosphere/reference/model.cc:140-237) hands them to "
-                             "RunJobs; the same sample (%.1f s wall)" % rows_wall}}
+    wall, sec = cpu_rebuild_seconds()
+    rows_wall, _ = cpu_rebuild_seconds(by_rows=True)
+    return {"value": 1.0 / wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "one whole config-0 Earth rebuild (4 orders, unsampled) by the FP64 "
+                      "oracle, %d threads on 64-texel blocks: %.1f s wall" % (cores, wall),
+            "reference_partition_rebuilds_per_s": 1.0 / rows_wall,
+            "pass_seconds": [round(x, 3) for x in sec]}
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (the FP64 oracle port of
+    atmosphere/reference/model.cc + functions.glsl) with every host thread:
+    each warm-up and each timed step is one whole, unsampled rebuild."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    stride = 64
-    for _ in range(args.warmup):
-        pass  # the CPU path has no warm-up state beyond the first call below
-    t0 = time.perf_counter()
-    totals = []
-    for _ in range(args.steps):
-        full, _, _ = cpu_rebuild_seconds(stride)
-        totals.append(full)
-    wall = time.perf_counter() - t0
-    value = len(totals) / sum(totals)
-    rows_full, _, _ = cpu_rebuild_seconds(stride, by_rows=True)
     cores = os.cpu_count() or 1
+    t_warm = time.perf_counter()
+    for _ in range(args.warmup):
+        cpu_rebuild_seconds()
+    warm_s = time.perf_counter() - t_warm
+    walls = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        wall, _ = cpu_rebuild_seconds()
+        walls.append(wall)
+    total = time.perf_counter() - t0
+    value = args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * sum(totals) / len(totals), "higher_is_better": True,
+        "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "batch": 1, "implementation":
-                   "CPU oracle port of atmosphere/reference/model.cc (FP64, all host threads)"},
+        "config": {"workload": WORKLOAD, "batch": 1, "orders": 4,
+                   "implementation": "CPU oracle port of atmosphere/reference/model.cc "
+                                     "(FP64, all host threads, 64-texel blocks)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "per step: one rebuild with density/multiple scattering on "
-                                   "every %dth texel, scaled, threads taking 64-texel blocks; "
-                                   "%.1f s wall for %d steps" % (stride, wall, args.steps),
-                         "reference_partition": {
-                             "value": 1.0 / rows_full, "unit": UNIT,
-                             "partition": "whole texture rows and r-slices per thread, as the "
-                                          "reference's CPU driver hands them to RunJobs "
-                                          "(atmosphere/reference/model.cc:140-237); one rebuild "
-                                          "of the same sample"}},
+                         "sample": "every step one whole, unsampled rebuild; %d warm-up "
+                                   "rebuilds (%.0f s), %d timed (%.0f s, min %.1f s, max "
+                                   "%.1f s per rebuild)" % (args.warmup, warm_s, args.steps,
+                                                            total, min(walls), max(walls))},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(rnd(line, 6)), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -377,8 +397,13 @@ def run_gpu(args):
 
     # --- roofline of the scattering-density kernel ---------------------------
     peak = atmo.measure_fp32_peak()
-    roof = roofline_entry(batch, B, peak, stream, value / world)
+    roof, passes_ms = roofline_entry(batch, B, peak, stream, value / world)
     del batch, single
+    torch.cuda.empty_cache()
+
+    # --- the spectral-precision and high-resolution configurations ----------
+    configs = {"spectral_fp16": run_spectral(atmo, W, torch, stream),
+               "hires_8_orders": run_hires(atmo, W, torch, stream)}
     torch.cuda.empty_cache()
 
     # --- mixed batch (uneven shapes and order counts) and serving -----------
@@ -388,35 +413,56 @@ def run_gpu(args):
     clk = clocks.summary()
     if rank != 0:
         return
+    north = {"single_p50_ms": p50, "single_p99_ms": p99, "plain_ms": plain_ms,
+             "plain_rebuilds_per_s": 1000.0 / plain_ms,
+             "batched_vs_plain": value / (1000.0 / plain_ms) / world,
+             "targets": "batched >= 50x plain (missed), single < 5 ms"}
+    cpu = cpu_baseline_entry() if not args.no_cpu_baseline else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: Earth parameters of the reference demo (no dataset)",
+        "data": "synthetic: Earth parameters of the reference demo",
+        "north_star": north,
         "config": {"workload": WORKLOAD, "batch": B, "orders": 4,
-                   "lut_shape": list(shape), "tuning": tuning,
                    "parallelism": "replicas (independent batches "
                    "per GPU)" if world > 1 else "single GPU",
                    "l2": "no flush: each step's working set (%d MB) exceeds the 129 MB L2"
-                         % (B * 64),
-                   "warm_up": {"steps": warm_steps, "seconds": round(warm_s, 2)}},
+                         % (B * 64)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "single_rebuild": {"p50_ms": p50, "p99_ms": p99, "fast_rebuilds_per_s": 1000.0 / p50,
-                           "plain_ms": plain_ms, "plain_rebuilds_per_s": 1000.0 / plain_ms,
-                           "batched_vs_plain": value / (1000.0 / plain_ms) / world},
-        "roofline": roof,
-        "parity": parity,
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clk,
+        "roofline": roof,
     }
+    if cpu:
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line["parity_max"] = {k: parity[k]["max"] for k in ("transmittance", "scattering",
+                                                         "irradiance") if k in parity}
+    line["configs"] = {k: {"ms": v.get("ms"), "max_err": v.get("max_err")}
+                       for k, v in configs.items()}
     if mixed:
-        line["batched_mixed"] = mixed
+        line["batched_mixed"] = {"rebuilds_per_s": mixed["rebuilds_per_s"],
+                                 "kernels": mixed["kernels_per_run"]}
     if serving:
-        line["serving"] = serving
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_entry()
-    print(json.dumps(line), flush=True)
+        line["serving"] = {"req_per_s": serving["throughput_req_per_s"],
+                           "rebuild_p50_p99_ms": [serving["rebuild_ms"]["p50"],
+                                                  serving["rebuild_ms"]["p99"]],
+                           "shade_p50_p99_ms": [serving["shade_ms"]["p50"],
+                                                serving["shade_ms"]["p99"]]}
+    detail = {"config": {"lut_shape": list(shape), "tuning": tuning,
+                         "warm_up": {"steps": warm_steps, "seconds": round(warm_s, 2)}},
+              "north_star": north, "roofline": roof, "passes_ms": passes_ms,
+              "parity": parity, "configs": configs, "batched_mixed": mixed,
+              "serving": serving, "cpu_baseline": cpu}
+    detail = rnd(detail, 6)
+    print("detail: " + json.dumps(detail), file=sys.stderr, flush=True)
+    out_dir = os.environ.get("ATMO_BENCH_OUT")
+    if out_dir:
+        os.makedirs(out_dir, exist_ok=True)
+        with open(os.path.join(out_dir, "bench_detail.json"), "w") as f:
+            json.dump(detail, f, indent=1)
+    print(json.dumps(rnd(line)), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -442,51 +488,35 @@ def time_plain(atmo, W, torch, stream, args):
 
 
 def roofline_entry(batch, B, peak, stream, rebuilds_per_s):
+    """The density kernel's FP32 roofline: executed FLOPs per second over the
+    measured FP32 FMA peak; its DRAM bytes against the compulsory ones."""
     passes = batch.time_passes(stream)
     dens = [(o, ms) for name, o, ms in passes if name == "scattering_density"]
     total = sum(ms for _, _, ms in passes)
     # One launch covers B instances x 1,048,576 texels x 512 directions.
     samples = B * 1048576 * 512
     dens_ms = sum(ms for _, ms in dens)
+    executed = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
+    achieved = executed / (dens_ms * 1e-3) / 1e12
     ref_per_sample, ref_rebuild = reference_flops()
     algorithmic = sum(ref_per_sample[min(o, 3)] * samples for o, _ in dens)
-    achieved = algorithmic / (dens_ms * 1e-3) / 1e12
-    executed = sum(DENSITY_FLOPS_PER_SAMPLE[min(o, 3)] * samples for o, _ in dens)
-    executed_rate = executed / (dens_ms * 1e-3) / 1e12
-    traffic = sum(DENSITY_DRAM_BYTES_PER_INSTANCE[min(o, 3)] * B for o, _ in dens) / len(dens)
-    hbm, hbm_source = hbm_peak()
-    dram_gbs = traffic / (dens_ms / len(dens) * 1e-3) / 1e9
-    return {"bound": "fp32", "kernel": "scattering density",
+    scale = B / 16.0
+    measured = [DENSITY_DRAM_BYTES_B16[min(o, 3)] for o, _ in dens]
+    traffic = (sum(measured) * scale / len(dens)) if all(m is not None for m in measured) \
+        else None
+    compulsory = sum(DENSITY_COMPULSORY_BYTES[min(o, 3)] * B for o, _ in dens) / len(dens)
+    hbm, _ = hbm_peak()
+    launch_s = dens_ms / len(dens) * 1e-3
+    roof = {"bound": "fp32", "kernel": "scattering density (k_density_fast, all orders)",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "flops": "the reference algorithm's: adds and muls of ComputeScatteringDensity "
-                     "per direction sample, counted in the oracle (%s); the restructured "
-                     "kernel executes fewer (see executed), so frac exceeds 1"
-                     % os.path.relpath(FLOPS_CONFIG0, ROOT),
-            "algorithmic_flops_per_sample": {str(k): round(v, 2)
-                                             for k, v in sorted(ref_per_sample.items())},
-            "executed": {"flops_per_sample": {str(k): v
-                                              for k, v in DENSITY_FLOPS_PER_SAMPLE.items()},
-                         "achieved": executed_rate, "frac": executed_rate / peak,
-                         "source": "ncu SASS op counters (FADD + FMUL + 2 FFMA + 2 FADD2 + "
-                                   "4 FFMA2) of one launch"},
-            "rebuild": {"algorithmic_flops": ref_rebuild,
-                        "achieved": ref_rebuild * rebuilds_per_s / 1e12,
-                        "frac": ref_rebuild * rebuilds_per_s / 1e12 / peak,
-                        "note": "all passes of one rebuild, reference-algorithm FLOPs x the "
-                                "batched rebuilds/s"},
-            "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2-instance "
-                              "launch per order (profiles/fast_kernels_earth_default_batch2.md), "
-                              "scaled to %d instances; bytes per launch, averaged over the "
-                              "step's density launches" % B,
-            "dram": {"bytes_per_launch": traffic, "achieved_gbs": dram_gbs, "peak_gbs": hbm,
-                     "frac": dram_gbs / hbm, "peak_source": hbm_source},
-            "peak_source": "FP32 FMA throughput measured in this run by atmo_measure_fp32_peak "
-                           "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
-            "avg_launch_ms": dens_ms / len(dens), "launches_per_step": len(dens),
-            "share_of_step": dens_ms / total,
-            "passes_ms": {n + ("" if o == 0 else str(o)): round(ms, 4)
-                          for n, o, ms in passes}}
+            "peak_source": "measured FP32 FMA rate (atmo_measure_fp32_peak)",
+            "traffic": traffic, "compulsory_bytes": compulsory,
+            "dram_frac": (traffic / launch_s / 1e9 / hbm) if traffic else None,
+            "avg_launch_ms": dens_ms / len(dens), "share_of_step": dens_ms / total,
+            "algorithmic_rate": {"tflops": algorithmic / (dens_ms * 1e-3) / 1e12,
+                                 "rebuild_tflops": ref_rebuild * rebuilds_per_s / 1e12}}
+    passes_ms = {n + ("" if o == 0 else str(o)): round(ms, 4) for n, o, ms in passes}
+    return roof, passes_ms
 
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "earth_default.npz")
@@ -524,6 +554,87 @@ def parity_entry(atmo, W, batch, torch):
     return out
 
 
+SPECTRAL_GOLDEN = os.path.join(ROOT, "tests", "golden", "spectral_default.npz")
+HIRES_GOLDEN = os.path.join(ROOT, "tests", "golden", "hires_earth.npz")
+
+
+def sampled_error(got, ref, idx=None, channels=3):
+    """(max, p99) relative error of got (float32 RGBA texels) at the golden
+    texels, with a floor of 1e-6 x the channel's and the texel's largest
+    value (the sRGB channels of the spectral configuration can be
+    cancellations of terms as large as the texel's largest channel)."""
+    g = np.asarray(got, np.float64).reshape(-1, 4)
+    if idx is not None:
+        g = g[idx]
+    r = np.asarray(ref, np.float64).reshape(-1, 4)[:, :channels]
+    g = g[:, :channels]
+    floor = np.maximum(PARITY_FLOOR * np.maximum(np.abs(r).max(axis=0), 1e-300),
+                       PARITY_FLOOR * np.abs(r).max(axis=1, keepdims=True))
+    rel = np.abs(g - r) / np.maximum(np.abs(r), floor)
+    return float(rel.max()), float(np.quantile(rel, 0.99))
+
+
+def time_events(torch, stream, fn, reps=3):
+    """Median CUDA-event time (ms) of fn() on `stream` over reps runs."""
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        out.append(a.elapsed_time(b))
+    return sorted(out)[len(out) // 2]
+
+
+def run_spectral(atmo, W, torch, stream):
+    """The spectral-precision configuration: 15 wavelengths in 5 groups of 3,
+    FP16 LUTs, the reference's default shape, 4 orders, through Model.Init;
+    error against the FP64 GPU oracle's committed sampled texels (bound:
+    1e-4 / 1e-3 plus FP16's 2^-11 on the stored scattering values)."""
+    m = W.spectral_earth_model(W.DEFAULT)
+    m.Init(4, stream=stream)
+    ms = time_events(torch, stream, lambda: m.Init(4, stream=stream, synchronize=False))
+    out = {"ms": ms, "wavelengths": 15, "groups": 5, "storage": "fp16"}
+    if os.path.exists(SPECTRAL_GOLDEN):
+        g = np.load(SPECTRAL_GOLDEN)
+        errs = {"T": sampled_error(m.transmittance(), g["transmittance"],
+                                   g["transmittance_index"]),
+                "S": sampled_error(m.scattering(), g["scattering"], g["scattering_index"]),
+                "M": sampled_error(m.single_mie_scattering(), g["single_mie"],
+                                   g["scattering_index"]),
+                "I": sampled_error(m.irradiance(), g["irradiance"])}
+        out["max_err"] = {k: v[0] for k, v in errs.items()}
+        out["p99_err"] = {k: v[1] for k, v in errs.items()}
+        out["reference"] = "FP64 GPU oracle, tests/golden/spectral_default.npz"
+    del m
+    return out
+
+
+def run_hires(atmo, W, torch, stream):
+    """The high-resolution configuration: scattering NU16 x MU_S64 x MU256 x
+    R64, transmittance 512x128, irradiance 128x32, 8 orders, one instance,
+    replayed as a CUDA graph; error against the FP64 GPU oracle's committed
+    sampled texels."""
+    b = atmo.Batch([W.hires_earth()], [W.HIRES], 8, combined=True)
+    b.run(stream)
+    ms = time_events(torch, stream, lambda: b.run(stream))
+    out = {"ms": ms, "orders": 8, "kernels": b.kernel_count()}
+    if os.path.exists(HIRES_GOLDEN):
+        torch.cuda.synchronize()
+        g = np.load(HIRES_GOLDEN)
+        errs = {"T": sampled_error(b.read(0, atmo.LUT_TRANSMITTANCE), g["transmittance"],
+                                   g["transmittance_index"]),
+                "S": sampled_error(b.read(0, atmo.LUT_SCATTERING), g["scattering"],
+                                   g["scattering_index"], channels=4),
+                "I": sampled_error(b.read(0, atmo.LUT_IRRADIANCE), g["irradiance"])}
+        out["max_err"] = {k: v[0] for k, v in errs.items()}
+        out["p99_err"] = {k: v[1] for k, v in errs.items()}
+        out["reference"] = "FP64 GPU oracle, tests/golden/hires_earth.npz"
+    del b
+    return out
+
+
 def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
     """The batched configuration: n seeded planets with shapes from {half,
     default, double-R} and 2-6 orders in one pass sequence (CUDA graph)."""
@@ -552,6 +663,36 @@ def run_mixed_batch(atmo, W, torch, stream, n=256, seed=3):
            "mean_orders": float(np.mean([o for _, _, o in reqs])), "tunings": tunings}
     del b
     torch.cuda.empty_cache()
+    return out
+
+
+def ticket_split(info):
+    """A request's latency split: queue (submission to admission: budget,
+    instance rows, batching window), launch (admission to its first kernel's
+    enqueue), device (GPU time of the launches it took part in) and the rest
+    (waiting on the GPU behind other work)."""
+    d = {"total": info.latency_ms, "queue": info.queue_ms,
+         "launch": max(info.launch_ms - info.queue_ms, 0.0) if info.launch_ms >= 0 else 0.0,
+         "device": max(info.device_ms, 0.0), "rounds": info.rounds}
+    d["wait"] = max(d["total"] - d["queue"] - d["launch"] - d["device"], 0.0)
+    return d
+
+
+def latency_breakdown(lat, split, pct):
+    """p50 / p99 of a request type's latency, and the mean split of the
+    requests at or above the p99 against that of all requests."""
+    out = {"p50": pct(lat, 0.5), "p99": pct(lat, 0.99), "n": len(lat)}
+    if not split:
+        return out
+    keys = ("queue", "launch", "device", "wait", "rounds")
+    p99 = out["p99"]
+    tail = [d for d in split if d["total"] >= p99] or split
+    out["mean_split"] = {k: float(np.mean([d[k] for d in split])) for k in keys}
+    out["p99_tail_split"] = {k: float(np.mean([d[k] for d in tail])) for k in keys}
+    out["queue_p50_p99"] = [pct([d["queue"] for d in split], 0.5),
+                            pct([d["queue"] for d in split], 0.99)]
+    out["device_p50_p99"] = [pct([d["device"] for d in split], 0.5),
+                             pct([d["device"] for d in split], 0.99)]
     return out
 
 
@@ -614,6 +755,7 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
             records.append(("shade", tk, time.perf_counter() - t0))
     submit_end = time.perf_counter() - t0
     lat = {"rebuild": [], "shade": []}
+    split = {"rebuild": [], "shade": []}
     end = 0.0
     failed = 0
     for kind, tk, ts in records:
@@ -623,6 +765,7 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
             failed += 1
             continue
         lat[kind].append(info.latency_ms)
+        split[kind].append(ticket_split(info))
         end = max(end, ts + info.latency_ms * 1e-3)
     st = srv.stats()
     srv.close()
@@ -638,10 +781,8 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
         "throughput_req_per_s": done / end if end > 0 else None,
         "rebuilds_per_s": len(lat["rebuild"]) / end if end > 0 else None,
         "shades_per_s": len(lat["shade"]) / end if end > 0 else None,
-        "rebuild_ms": {"p50": pct(lat["rebuild"], 0.5), "p99": pct(lat["rebuild"], 0.99),
-                       "n": len(lat["rebuild"])},
-        "shade_ms": {"p50": pct(lat["shade"], 0.5), "p99": pct(lat["shade"], 0.99),
-                     "n": len(lat["shade"])},
+        "rebuild_ms": latency_breakdown(lat["rebuild"], split["rebuild"], pct),
+        "shade_ms": latency_breakdown(lat["shade"], split["shade"], pct),
         "view": "1920x1080, FOV 50 deg: GetSkyRadiance, GetSkyRadianceToPoint and "
                 "GetSunAndSkyIrradiance per pixel",
         "server": {"rounds": st.rounds, "kernels": st.kernels, "evictions": st.evictions,

@@ -10,7 +10,7 @@ import math
 
 import numpy as np
 
-from . import Atmosphere, PinholeView
+from . import Atmosphere, DensityProfileLayer, Model, PinholeView
 
 DEFAULT = (256, 64, 32, 128, 32, 8, 64, 16)      # atmosphere/constants.h:47-61
 HALF = (128, 32, 16, 64, 16, 4, 32, 8)           # every size halved
@@ -101,3 +101,48 @@ def random_view(rng, bottom_radius, width=1920, height=1080, fov_deg=50.0) -> Pi
     v.fov_y = math.radians(fov_deg)
     v.width, v.height = width, height
     return v
+
+
+def smooth_solar_spectrum(seed, wavelengths):
+    """A seeded smooth solar spectrum in [1, 2] W/m^2/nm at `wavelengths`
+    (nm): 1.5 plus four random sines over 360-830 nm, clipped."""
+    rng = np.random.default_rng(seed)
+    x = (np.asarray(wavelengths, np.float64) - 360.0) / 470.0
+    s = 1.5 + sum(rng.uniform(0.05, 0.12) * np.sin(2 * np.pi * rng.uniform(0.5, 3.0) * x +
+                                                   rng.uniform(0, 2 * np.pi)) for _ in range(4))
+    return np.clip(s, 1.0, 2.0)
+
+
+# Ozone absorption cross sections (m^2) at 360, 370, ..., 830 nm.
+OZONE_CROSS_SECTION_10NM = np.array([
+    1.18e-27, 2.182e-28, 2.818e-28, 6.636e-28, 1.527e-27, 2.763e-27, 5.52e-27, 8.451e-27,
+    1.582e-26, 2.316e-26, 3.669e-26, 4.924e-26, 7.752e-26, 9.016e-26, 1.48e-25, 1.602e-25,
+    2.139e-25, 2.755e-25, 3.091e-25, 3.5e-25, 4.266e-25, 4.672e-25, 4.398e-25, 4.701e-25,
+    5.019e-25, 4.305e-25, 3.74e-25, 3.215e-25, 2.662e-25, 2.238e-25, 1.852e-25, 1.473e-25,
+    1.209e-25, 9.423e-26, 7.455e-26, 6.566e-26, 5.105e-26, 4.15e-26, 4.228e-26, 3.237e-26,
+    2.451e-26, 2.801e-26, 2.534e-26, 1.624e-26, 1.465e-26, 2.078e-26, 1.383e-26, 7.105e-27])
+
+
+def spectral_earth_model(shape=None, seed=1, num_precomputed_wavelengths=15,
+                         combine_scattering_textures=False, half_precision=True) -> Model:
+    """The spectral-precision configuration: the demo's Earth tabulated every
+    10 nm over 360-830 nm with a seeded smooth solar spectrum, 15 precomputed
+    wavelengths (5 groups of 3), FP16 LUT storage, separate single-Mie LUT."""
+    w = np.arange(360.0, 831.0, 10.0)
+    lam = w * 1e-3
+    mie = 5.328e-3 / 1200.0 * np.ones_like(w)
+    L = DensityProfileLayer
+    return Model(w, smooth_solar_spectrum(seed, w), 0.00935 / 2.0, 6360e3, 6420e3,
+                 [L(0.0, 1.0, -1.0 / 8000.0, 0.0, 0.0)], 1.24062e-6 * lam ** -4,
+                 [L(0.0, 1.0, -1.0 / 1200.0, 0.0, 0.0)], mie * 0.9, mie, 0.8,
+                 [L(25000.0, 0.0, 0.0, 1.0 / 15000.0, -2.0 / 3.0),
+                  L(0.0, 0.0, 0.0, -1.0 / 15000.0, 8.0 / 3.0)],
+                 300.0 * 2.687e20 / 15000.0 * OZONE_CROSS_SECTION_10NM, np.full_like(w, 0.1),
+                 102.0 / 180.0 * math.pi, 1000.0, num_precomputed_wavelengths,
+                 combine_scattering_textures, half_precision, lut_shape=shape)
+
+
+def hires_earth() -> Atmosphere:
+    """The high-resolution configuration's atmosphere: the demo's Earth with
+    Mie g = 0.76 and ground albedo 0.3 (LUT shape HIRES, 8 orders)."""
+    return earth(mie_g=0.76, albedo=0.3)
