@@ -391,6 +391,12 @@ def run_gpu(args):
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
     plain_ms = time_plain(atmo, W, torch, stream, args)
+    # The single rebuild's kernels timed one by one (no graph): their sum
+    # against the graph replay's p50 is the cost of the launch boundaries.
+    single_passes = single.time_passes(stream)
+    launch_gaps = {"graph_p50_ms": p50,
+                   "sum_of_kernels_ms": sum(ms for _, _, ms in single_passes),
+                   "kernels": len(single_passes)}
 
     # --- error of the benchmarked LUTs against the FP64 reference ------------
     parity = parity_entry(atmo, W, batch, torch)
@@ -452,7 +458,8 @@ def run_gpu(args):
                                                 serving["shade_ms"]["p99"]]}
     detail = {"config": {"lut_shape": list(shape), "tuning": tuning,
                          "warm_up": {"steps": warm_steps, "seconds": round(warm_s, 2)}},
-              "north_star": north, "roofline": roof, "passes_ms": passes_ms,
+              "north_star": north, "launch_gaps": launch_gaps, "roofline": roof,
+              "passes_ms": passes_ms,
               "parity": parity, "configs": configs, "batched_mixed": mixed,
               "serving": serving, "cpu_baseline": cpu}
     detail = rnd(detail, 6)

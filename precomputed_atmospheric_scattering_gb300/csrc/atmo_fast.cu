@@ -76,6 +76,32 @@ __device__ __forceinline__ P3 Fma(P3 a, P3 b, P3 c) {
 }
 __device__ __forceinline__ P3 Add(P3 a, P3 b) { return P3{__fadd2_rn(a.xy, b.xy), a.z + b.z}; }
 
+// Approximate reciprocal square root, square root and division that flush
+// subnormal operands to zero (the PTX .approx.ftz forms).  The non-flushing
+// forms that rsqrtf, sqrtf under --prec-sqrt=false and __fdividef compile to
+// add a range check and a rescaling of subnormal operands to every call.
+// Every operand given to these below is zero, a normal number or negative
+// (where both forms return NaN); on normal operands of the ranges used here
+// the two forms agree bit for bit (16.7 M operands per range compared on a
+// GB300).  Single and multiple scattering take 4.5% and 3.8% less time; their
+// LUTs are not bit-identical to the non-flushing build's (the code around the
+// calls is scheduled and contracted differently) and meet the same bounds.
+__device__ __forceinline__ float RsqrtFtz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float SqrtFtz(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float DivFtz(float a, float b) {
+  float y;
+  asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(y) : "f"(a), "f"(b));
+  return y;
+}
+
 // a b + c clamped to [0, 1], NaN to 0 (one FMA with the .sat modifier).
 __device__ __forceinline__ float FmaSat(float a, float b, float c) {
   float d;
@@ -293,7 +319,8 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
     // with the scattering coefficients into one weight per channel.
     const float nu2 = fmaf(oxs, cs.x, B);
     const float q2 = fmaf(nu2, nu2, 1.0f);
-    const float rs = rsqrtf(fmaf(m2g, nu2, g2p1));
+    // 1 + g^2 - 2 g nu2 >= (1 - g)^2: zero or normal for |g| < 1.
+    const float rs = RsqrtFtz(fmaf(m2g, nu2, g2p1));
     const F3 wf = fma3(wam, q2 * (rs * rs * rs), war * q2);
     const P3 w = ToP3(wf);
     const float hc = cs.x * hs, hn = cs.y * hs;
@@ -326,7 +353,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
           // (1 + nu1^2) (R 3/(16 pi) + M k_M / (1 + g^2 - 2 g nu1)^(3/2)),
           // with the constant factors staged into the tables.
           const float nu1 = fmaf(u, inv_k1, -0.5f * inv_k1);
-          const float r1 = rsqrtf(fmaf(m2g, nu1, g2p1));
+          const float r1 = RsqrtFtz(fmaf(m2g, nu1, g2p1));
           const F3 L1 = fma3(M, r1 * r1 * r1, L);
           const float q1 = fmaf(nu1, nu1, 1.0f);
           Ls = side == 0 ? L1 * q1 : fma3(L1, q1, Ls);
@@ -693,10 +720,13 @@ __device__ __forceinline__ float UMuSFromMuSAlongRay(const Consts& c, const Shap
                                                      float inv_range, float inv_A) {
   const float H2 = c.H * c.H;
   const float rmus = c.Rb * mu_s;
-  const float sq = sqrtf(fmaf(rmus, rmus, H2));
-  const float d = rmus > 0.0f ? __fdividef(H2, rmus + sq) : sq - rmus;
+  // H^2 + (Rb mu_s)^2 >= H^2 and rmus + sq >= H > 0: normal.  The last
+  // quotient's numerator is zero or in [ulp(1), 1], its denominator in
+  // [1, 2].
+  const float sq = SqrtFtz(fmaf(rmus, rmus, H2));
+  const float d = rmus > 0.0f ? DivFtz(H2, rmus + sq) : sq - rmus;
   const float a = (d - (c.Rt - c.Rb)) * inv_range;
-  return TexCoord(s, kMapSMUS, __fdividef(fmaxf(fmaf(-a, inv_A, 1.0f), 0.0f), 1.0f + a));
+  return TexCoord(s, kMapSMUS, DivFtz(fmaxf(fmaf(-a, inv_A, 1.0f), 0.0f), 1.0f + a));
 }
 
 template <int kCols>
@@ -1009,12 +1039,16 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
           const float st = clampf((rmu + sm.rho) * sm.inv_r * sm.inv_2e + 0.5f, 0.0f, 1.0f);
           const float sun = st * st * fmaf(-2.0f, st, 3.0f);
           const float delta = (sm.rho - rmu) * (sm.rho + rmu);
-          const float sq = sqrtf(fmaxf(H2 - delta, 0.0f));
+          // H^2 - delta: zero, or a difference of floats far above FP32's
+          // normal range (normal); delta and rho - rmu: zero, or sums and
+          // products of lengths whose exact values are multiples of their
+          // operands' ulps (normal); H + sq >= H.
+          const float sq = SqrtFtz(fmaxf(H2 - delta, 0.0f));
           const float rho_minus_a =
-              rmu < 0.0f ? (sm.rho - rmu > 0.0f ? __fdividef(delta, sm.rho - rmu) : 0.0f)
+              rmu < 0.0f ? (sm.rho - rmu > 0.0f ? DivFtz(delta, sm.rho - rmu) : 0.0f)
                          : sm.rho + rmu;
           const float omx =
-              clampf((rho_minus_a + __fdividef(delta, H + sq)) * sm.inv_range, 0.0f, 1.0f);
+              clampf((rho_minus_a + DivFtz(delta, H + sq)) * sm.inv_range, 0.0f, 1.0f);
           const float Xc = omx * tw1;
           const float f = floorf(Xc);
           const float gw = Xc - f;   // weight of the lower column
