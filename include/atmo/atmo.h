@@ -420,6 +420,9 @@ typedef struct {
                                         (0: the device's default); a rebuild admitted under
                                         the budget that the pool cannot serve fails with
                                         ATMO_OOM */
+  unsigned max_shades_in_flight;     /* shading kernels enqueued and not complete at once
+                                        (0: no cap); a cap keeps SMs free for the rebuild
+                                        rounds at the cost of queueing shading on the host */
 } atmo_server_config;
 typedef struct {
   int state;             /* 0 queued, 1 running, 2 done, 3 failed (or cancelled) */

@@ -141,7 +141,8 @@ class Tuning(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_rebuilds_in_flight", C.c_uint),
                 ("shade_streams", C.c_uint), ("combined", C.c_int),
-                ("admit_window_us", C.c_uint), ("pool_max_bytes", C.c_size_t)]
+                ("admit_window_us", C.c_uint), ("pool_max_bytes", C.c_size_t),
+                ("max_shades_in_flight", C.c_uint)]
 
 
 class TicketInfo(C.Structure):
@@ -565,9 +566,10 @@ class Server:
     QUEUED, RUNNING, DONE, FAILED = range(4)
 
     def __init__(self, hbm_budget_bytes=0, max_rebuilds_in_flight=0, shade_streams=0,
-                 combined=True, admit_window_us=0, pool_max_bytes=0):
+                 combined=True, admit_window_us=0, pool_max_bytes=0, max_shades_in_flight=0):
         cfg = ServerConfig(hbm_budget_bytes, max_rebuilds_in_flight, shade_streams,
-                           int(bool(combined)), admit_window_us, pool_max_bytes)
+                           int(bool(combined)), admit_window_us, pool_max_bytes,
+                           max_shades_in_flight)
         h = C.c_void_p()
         _check(lib().atmo_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -568,6 +568,7 @@ bool atmo_server::RetireRounds() {
 bool atmo_server::LaunchShades() {
   bool any = false;
   for (auto it = pending_shades.begin(); it != pending_shades.end();) {
+    if (cfg.max_shades_in_flight > 0 && shades.size() >= cfg.max_shades_in_flight) break;
     auto si = slots.find(it->set_id);
     if (si == slots.end()) {
       // A rebuild still queued for admission (batching window, budget) has
