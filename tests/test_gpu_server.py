@@ -289,3 +289,29 @@ def test_cancel_a_running_rebuild_releases_its_budget(atmo, oracle, torch_cuda):
         assert st.building == 0 and 0 < st.used_bytes <= one_set
     finally:
         srv.close()
+
+
+@pytest.mark.gpu
+def test_shading_cap_changes_scheduling_not_results(atmo, oracle, torch_cuda):
+    """max_shades_in_flight = 1 queues shading on the host: every request
+    still completes, with the same pixels as without the cap."""
+    torch = torch_cuda
+    outs = []
+    for cap in (0, 1):
+        srv = atmo.Server(max_shades_in_flight=cap)
+        try:
+            set_id = srv.submit_rebuild(oracle.earth_atmosphere(), SMALL, 3)
+            tickets, keep = [], []
+            for seed in range(5):
+                view, depth = make_view(atmo, 10 + seed)
+                t, k = shade(torch, srv, set_id, view, depth)
+                tickets.append(t)
+                keep.append(k)
+            for t in tickets:
+                assert srv.wait(t, 60000).state == atmo.Server.DONE
+            torch.cuda.synchronize()
+            outs.append([torch.cat([k[1].flatten(), k[2].flatten()]) for k in keep])
+        finally:
+            srv.close()
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
