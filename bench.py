@@ -729,11 +729,13 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
     # One shading request alone, on the default stream (CUDA events, median of 5).
     lone = srv.lut_set(earth_id)
     stream = torch.cuda.current_stream()
-    shade_alone_ms = time_events(torch, stream, lambda: lone.shade_view(
-        W.random_view(np.random.default_rng(0), 6360.0), depth, stream=stream), reps=5)
+    lone_view = W.random_view(np.random.default_rng(0), 6360.0)
+    lone.shade_view(lone_view, depth, stream=stream)
+    shade_alone_ms = time_events(torch, stream,
+                                 lambda: lone.shade_view(lone_view, depth, stream=stream), reps=5)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.2) + 16))
     arrivals = arrivals[arrivals < seconds]
-    building, records = [], []
+    building, records, kinds = [], [], []
     nslot = 0
     t0 = time.perf_counter()
     for ta in arrivals:
@@ -755,6 +757,7 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
             radius[tk] = a.bottom_radius
             building.append(tk)
             records.append(("rebuild", tk, time.perf_counter() - t0))
+            kinds.append((tuple(shape), orders, a))
         else:
             set_id = ready[int(rng.integers(0, len(ready)))]
             j = nslot % pool
@@ -781,6 +784,17 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
         end = max(end, ts + info.latency_ms * 1e-3)
     st = srv.stats()
     srv.close()
+    # Each rebuild's own GPU time alone (one instance of its LUT shape and
+    # order count, CUDA-graph replay, median of 3): the spread of the work
+    # itself, beside the latencies.
+    lone = {}
+    for shape, orders, a in kinds:
+        if (shape, orders) not in lone:
+            b = atmo.Batch([a], [shape], orders)
+            b.run(stream)
+            lone[(shape, orders)] = time_events(torch, stream, lambda: b.run(stream))
+            del b
+    lone_ms = sorted(lone[(shape, orders)] for shape, orders, _ in kinds)
 
     def pct(xs, q):
         xs = sorted(xs)
@@ -799,9 +813,12 @@ def run_serving(atmo, W, torch, seconds, rate=2000.0, rebuild_fraction=0.1, seed
                 "GetSunAndSkyIrradiance per pixel",
         "max_shades_in_flight": max_shades_in_flight,
         "shade_alone_ms": shade_alone_ms,
+        "rebuild_alone_ms": {"p50": pct(lone_ms, 0.5), "p99": pct(lone_ms, 0.99),
+                             "mean": float(np.mean(lone_ms)) if lone_ms else None},
         "offered_gpu_load": (rate * (1.0 - rebuild_fraction) * shade_alone_ms +
-                             (rate * rebuild_fraction * rebuild_alone_ms
-                              if rebuild_alone_ms else 0.0)) / 1000.0,
+                             rate * rebuild_fraction *
+                             (float(np.mean(lone_ms)) if lone_ms else (rebuild_alone_ms or 0.0))
+                             ) / 1000.0,
         "server": {"rounds": st.rounds, "kernels": st.kernels, "evictions": st.evictions,
                    "resident_sets": st.resident_sets, "used_gb": st.used_bytes / 2 ** 30,
                    "budget_gb": st.budget_bytes / 2 ** 30},

@@ -379,7 +379,9 @@ typedef struct {
    sky_rgba[pixel] = GetSkyRadiance(camera, view ray) (alpha: the green
    transmittance); shaded_rgba[pixel] = GetSkyRadianceToPoint(camera, p) +
    transmittance x albedo / pi x (sun + sky irradiance of GetSunAndSkyIrradiance
-   at p with normal -view ray), p = camera + depth[pixel] x view ray. */
+   at p with normal -view ray), p = camera + depth[pixel] x view ray.  The
+   radiance to p is integrated along the view ray itself (the query form takes
+   the direction of p - camera). */
 atmo_status atmo_shade_view(const atmo_lut_set* set, const atmo_pinhole_view* view,
                             const float* depth, int luminance, float* sky_rgba,
                             float* shaded_rgba, atmo_stream stream);
