@@ -350,14 +350,15 @@ def test_shade_view_equals_queries(atmo, torch):
     torch.testing.assert_close(got[~far], expect[~far], rtol=5e-2, atol=1e-6)
 
 
-def test_shade_view_vs_oracle(atmo, oracle, torch):
+@pytest.mark.parametrize("combined", [True, False], ids=["combined", "separate"])
+def test_shade_view_vs_oracle(atmo, oracle, torch, combined):
     """shade_view against the oracle's FP64 render functions along each
     pixel's exact ray (point = camera + depth x ray in FP64), on the pixels
     where the oracle is well conditioned (the robustness mask of the query
     tests), with the query tests' bounds: sky radiance within TOL_RENDER, the
     shaded value (radiance to the point plus the lit albedo) within
     TOL_RENDER of itself plus TOL_TERMS of the sky radiance along the ray."""
-    m = earth_model(atmo, combined=True)
+    m = earth_model(atmo, combined=combined)
     m.Init(4)
     s = m.lut_set()
     W, H = 48, 32
@@ -389,7 +390,8 @@ def test_shade_view_vs_oracle(atmo, oracle, torch):
     T = m.transmittance()
     S = m.scattering()
     I = m.irradiance()
-    ref = OracleRender(oracle, m.atmosphere_at(), atmo.DEFAULT_SHAPE, T, S, S, I, True)
+    M = S if combined else m.single_mie_scattering()
+    ref = OracleRender(oracle, m.atmosphere_at(), atmo.DEFAULT_SHAPE, T, S, M, I, combined)
     alb = f32(albedo).astype(np.float64) / np.pi
 
     def evaluate(perturb):
