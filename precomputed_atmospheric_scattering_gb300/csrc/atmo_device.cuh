@@ -563,6 +563,11 @@ struct IrrRow {          // one r row of the irradiance LUT
 
 struct Tables {
   TexelRow* rows;        // [sr * smu]
+  // [sr * smu] the order in which the multiple-scattering blocks take the
+  // rows (by the invariant delta of their rays, so that the rows in flight
+  // read the same delta-density rows), or nullptr: k-major order.  Any order
+  // gives the same LUTs.
+  int* row_order;
   TexelCol* cols;        // [smus]
   DensityRow* drows;     // [sr * 16]
   IrrRow* irows;         // [ih]

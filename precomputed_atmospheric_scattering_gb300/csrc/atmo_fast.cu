@@ -671,6 +671,11 @@ int MultipleFastSmem(const Shape& s) {
   return d.rows * kRaySamples * (int)sizeof(RaySample) + 2 * d.group * d.rows * s.sw() * 16;
 }
 
+// The LUT row that logical row i of the multiple-scattering blocks takes.
+__device__ __forceinline__ int RowAt(const Tables& tab, int i) {
+  return tab.row_order ? __ldg(tab.row_order + i) : i;
+}
+
 // Sample i of the ray of LUT row `rowi` (the per-sample part of
 // MultipleScatteringTexel that does not depend on mu_s or nu).
 __device__ RaySample MakeRaySample(const Instance& in, int rowi, int i) {
@@ -742,14 +747,14 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
 
   for (int e = threadIdx.x; e < R * kRaySamples; e += kMultipleFastThreads) {
     const int rr = e / kRaySamples, i = e - rr * kRaySamples;
-    if (row0 + rr < rows_total) samp[e] = MakeRaySample(in, row0 + rr, i);
+    if (row0 + rr < rows_total) samp[e] = MakeRaySample(in, RowAt(in.tab, row0 + rr), i);
   }
 
   // This thread's row within the tile and its texel columns x_t + 256 m.
   const int rr = kCols == 1 ? (int)threadIdx.x / W : 0;
   const int x_t = kCols == 1 ? (int)threadIdx.x - rr * W : (int)threadIdx.x;
-  const int rowi = row0 + rr;
-  const bool active = rr < R && rowi < rows_total;
+  const bool active = rr < R && row0 + rr < rows_total;
+  const int rowi = active ? RowAt(in.tab, row0 + rr) : 0;
   const float smus_f = float(s.smus);
   const int nmax = W - 1;
   const float inv_range = 1.0f / (c.H - (c.Rt - c.Rb));
