@@ -1053,28 +1053,20 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
     // Transmittance LUT rows j0, j1 of each sample, interpolated in rho.
     if (R == 1 && TW <= kMultipleFastThreads) {
       // One row per block, one line column per thread: consecutive samples
-      // of the ray read the same two LUT rows (39% at the reference's shape)
-      // or share one (53%), which stay in registers (49% fewer loads; the
-      // same values, hence the same LUTs).  Uniform branches: every thread
-      // takes the same sample.
+      // of the ray read the same two LUT rows 39% of the time at the
+      // reference's shape, and those rows, already in registers, are not
+      // loaded again (predicated loads: the same values, hence the same LUTs).
+      // Handling the samples that share one row as well (another 53%) with
+      // a branch per case, or with selects, measured slower.
       const int x = threadIdx.x;
       if (x < TW && row0 < rows_total) {
         int o0 = -1, o1 = -1;
-        float4 a, b;
+        float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
         for (int g = 0; g < count; ++g) {
           const SunSample& sm = samp[first + g];
-          if (sm.t0 == o0 && sm.t1 == o1) {
-            // the same two rows
-          } else if (sm.t0 == o1) {
-            a = b;
-            b = __ldg(in.T + sm.t1 + x);
-          } else if (sm.t1 == o0) {
-            b = a;
-            a = __ldg(in.T + sm.t0 + x);
-          } else {
-            a = __ldg(in.T + sm.t0 + x);
-            b = __ldg(in.T + sm.t1 + x);
-          }
+          const int fresh = (sm.t0 != o0) | (sm.t1 != o1);
+          LoadIf(a, in.T + sm.t0 + x, fresh);
+          LoadIf(b, in.T + sm.t1 + x, fresh);
           o0 = sm.t0;
           o1 = sm.t1;
           buf[g * TW + x] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
