@@ -503,6 +503,24 @@ atmo_status atmo_get_tuning(const atmo_lut_shape* shape, atmo_tuning* out);
    short dependent-chain kernel over every SM: the denominator of the
    precomputation kernels' FP32 roofline.  Synchronous, ~10 ms. */
 atmo_status atmo_measure_fp32_peak(double* tflops);
+/* Device-side access checks.  The reference checks its L0 functions with
+   asserts in its C++ Debug build and compiles them out of the shaders
+   (atmosphere/model.cc:698); here the checked build of this library
+   (libatmo_gb300_checked.so, compiled with -DATMO_DEVICE_CHECKS) tests the
+   indices the kernels compute -- shared-memory table lookups, line-build rows
+   and taps, staged texels, the texels of every LUT lookup -- against the
+   buffers they read, records the first failure and reads element 0 instead.
+   Reads (after a device synchronisation) and, with `reset`, clears the
+   record: *compiled = 1 in the checked build, 0 in the ordinary one (whose
+   record is always 0); *first_failure = 0 when every check passed, else the
+   failing site (top 8 bits: 1 shared-memory lookup, 2 LUT texel, 3 staged
+   texel, 4 line-build row, 5 line tap, 6 output texel, 255 self-test) and the
+   failing index (low 56 bits). */
+atmo_status atmo_device_checks(int reset, int* compiled, unsigned long long* first_failure);
+/* Launches one check that fails by construction (index 5 of 3, no memory
+   access) on `stream`: in the checked build the record then holds site 255,
+   index 5.  Tests the recording path without an invalid access. */
+atmo_status atmo_device_checks_selftest(atmo_stream stream);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,10 @@ import os
 import numpy as np
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libatmo_gb300.so")
+# ATMO_LIBRARY=checked loads the checked build (device-side index checks of
+# csrc/atmo_check.cuh, built on first use) instead of the ordinary one.
+CHECKED = os.environ.get("ATMO_LIBRARY", "") == "checked"
+LIB_PATH = os.path.join(_PKG, "libatmo_gb300_checked.so" if CHECKED else "libatmo_gb300.so")
 
 kLambdaR = 680.0
 kLambdaG = 550.0
@@ -176,10 +179,11 @@ class LutView(C.Structure):
 _lib = None
 
 
-def build(verbose=False, force=False):
-    """Compiles libatmo_gb300.so for sm_103a (nvcc)."""
+def build(verbose=False, force=False, checked=None):
+    """Compiles libatmo_gb300.so for sm_103a (nvcc); with checked (default:
+    the ATMO_LIBRARY setting), libatmo_gb300_checked.so."""
     from . import nvcc_build as _b
-    return _b.build(verbose=verbose, force=force)
+    return _b.build(verbose=verbose, force=force, checked=CHECKED if checked is None else checked)
 
 
 def lib():
@@ -187,8 +191,8 @@ def lib():
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             raise ImportError(
-                "libatmo_gb300.so is not built: run precomputed_atmospheric_scattering_gb300."
-                "build() (there is no CPU fallback)")
+                "%s is not built: run precomputed_atmospheric_scattering_gb300."
+                "build() (there is no CPU fallback)" % os.path.basename(LIB_PATH))
         L = C.CDLL(LIB_PATH)
         P, st = C.POINTER, C.c_int
         vp = C.c_void_p
@@ -253,6 +257,8 @@ def lib():
             "atmo_server_evict": [vp, C.c_uint64],
             "atmo_server_get_stats": [vp, P(ServerStats)],
             "atmo_autotune": [P(Atmosphere), P(LutShape), C.c_uint, P(Tuning)],
+            "atmo_device_checks": [C.c_int, P(C.c_int), P(C.c_ulonglong)],
+            "atmo_device_checks_selftest": [vp],
             "atmo_set_tuning": [P(LutShape), P(Tuning)],
             "atmo_get_tuning": [P(LutShape), P(Tuning)],
             "atmo_model_save_luts": [vp, C.c_char_p],
@@ -661,6 +667,28 @@ def measure_fp32_peak():
     t = C.c_double()
     _check(lib().atmo_measure_fp32_peak(C.byref(t)))
     return t.value
+
+
+CHECK_SITES = {1: "shared-memory lookup", 2: "LUT texel", 3: "staged texel",
+               4: "line-build row", 5: "line tap", 6: "output texel", 255: "self-test"}
+
+
+def device_checks(reset=False):
+    """The record of the checked build's device-side index checks (after a
+    device synchronisation; with reset, cleared): (compiled, failure), where
+    compiled is whether this library is the checked build and failure is None
+    when every check passed, else (site name, index) of the first failure."""
+    compiled, word = C.c_int(), C.c_ulonglong()
+    _check(lib().atmo_device_checks(int(bool(reset)), C.byref(compiled), C.byref(word)))
+    w = word.value
+    if w == 0:
+        return bool(compiled.value), None
+    return bool(compiled.value), (CHECK_SITES.get(w >> 56, str(w >> 56)), w & ((1 << 56) - 1))
+
+
+def device_checks_selftest(stream=None):
+    """Launches one check that fails by construction (index 5 of 3, no access)."""
+    _check(lib().atmo_device_checks_selftest(stream))
 
 
 def synchronize_stream(stream=None):

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/atmo/atmo.h"
+#include "atmo_check.cuh"
 #include "atmo_consts.h"
 #include "atmo_kernels.h"
 #include "atmo_program.h"
@@ -838,6 +839,28 @@ atmo_status atmo_batch_time_passes(atmo_batch* b, atmo_stream stream, unsigned c
 atmo_status atmo_measure_fp32_peak(double* tflops) {
   if (!tflops) return Fail(ATMO_INVALID_ARG, "NULL argument");
   ATMO_CUDA_TRY(MeasureFp32Peak(tflops));
+  return ATMO_OK;
+}
+
+atmo_status atmo_device_checks(int reset, int* compiled, unsigned long long* first_failure) {
+  if (!compiled || !first_failure) return Fail(ATMO_INVALID_ARG, "NULL argument");
+  *compiled = kDeviceChecks ? 1 : 0;
+  *first_failure = 0;
+  if (!kDeviceChecks) return ATMO_OK;
+  ATMO_CUDA_TRY(cudaDeviceSynchronize());
+  // One word per translation unit with kernels; the first nonzero one.
+  unsigned long long (*const words[4])(bool) = {CheckWordKernels, CheckWordRays,
+                                                CheckWordFast, CheckWordRender};
+  for (auto word : words) {
+    const unsigned long long w = word(reset != 0);
+    if (w == ~0ull) return Fail(ATMO_CUDA_ERROR, "reading a device check word");
+    if (*first_failure == 0) *first_failure = w;
+  }
+  return ATMO_OK;
+}
+
+atmo_status atmo_device_checks_selftest(atmo_stream stream) {
+  ATMO_CUDA_TRY(LaunchCheckSelfTest(reinterpret_cast<cudaStream_t>(stream)));
   return ATMO_OK;
 }
 

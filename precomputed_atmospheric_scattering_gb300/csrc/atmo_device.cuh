@@ -17,6 +17,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "atmo_check.cuh"
+
 #ifdef __CUDACC__
 #include <cuda_fp16.h>
 #define ATMO_HD __host__ __device__ __forceinline__
@@ -194,8 +196,10 @@ ATMO_HD F3 Bilinear(const float4* __restrict__ tex, int w, int h, float u, float
   j0 = j0 < 0 ? 0 : (j0 > h - 1 ? h - 1 : j0);
   j1 = j1 < 0 ? 0 : (j1 > h - 1 ? h - 1 : j1);
 #ifdef __CUDA_ARCH__
-  float4 t00 = __ldg(tex + j0 * w + i0), t10 = __ldg(tex + j0 * w + i1);
-  float4 t01 = __ldg(tex + j1 * w + i0), t11 = __ldg(tex + j1 * w + i1);
+  float4 t00 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, j0 * w, i0, w * h));
+  float4 t10 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, j0 * w, i1, w * h));
+  float4 t01 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, j1 * w, i0, w * h));
+  float4 t11 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, j1 * w, i1, w * h));
 #else
   float4 t00 = tex[j0 * w + i0], t10 = tex[j0 * w + i1];
   float4 t01 = tex[j1 * w + i0], t11 = tex[j1 * w + i1];
@@ -247,10 +251,10 @@ ATMO_HD TCoords TransmittanceCoords(const Consts& c, const Shape& s, float rho, 
   j0 = j0 < 0 ? 0 : (j0 > Hh - 1 ? Hh - 1 : j0);
   j1 = j1 < 0 ? 0 : (j1 > Hh - 1 ? Hh - 1 : j1);
   TCoords t;
-  t.i00 = j0 * W + i_lo;
-  t.i10 = j0 * W + i_hi;
-  t.i01 = j1 * W + i_lo;
-  t.i11 = j1 * W + i_hi;
+  t.i00 = (int)ATMO_CHECKED_INDEX(kCheckLutTexel, j0 * W + i_lo, W * Hh);
+  t.i10 = (int)ATMO_CHECKED_INDEX(kCheckLutTexel, j0 * W + i_hi, W * Hh);
+  t.i01 = (int)ATMO_CHECKED_INDEX(kCheckLutTexel, j1 * W + i_lo, W * Hh);
+  t.i11 = (int)ATMO_CHECKED_INDEX(kCheckLutTexel, j1 * W + i_hi, W * Hh);
   t.w00 = g * (1.0f - b);
   t.w10 = (1.0f - g) * (1.0f - b);
   t.w01 = g * b;
@@ -472,7 +476,7 @@ ATMO_HD F3 Scattering4(const float4* __restrict__ tex, const Shape& s, const Loo
     const int i0 = ClampIdx(base + (int)fx, W), i1 = ClampIdx(base + (int)fx + 1, W);
     const float wa0 = (1.0f - a) * wn, wa1 = a * wn;
 #ifdef __CUDA_ARCH__
-#define ATMO_TAP(idx) __ldg(tex + (idx))
+#define ATMO_TAP(idx) __ldg(tex + ATMO_CHECKED_INDEX(kCheckLutTexel, (idx), W * Hh * D))
 #else
 #define ATMO_TAP(idx) tex[(idx)]
 #endif

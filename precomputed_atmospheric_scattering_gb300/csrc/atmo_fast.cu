@@ -109,8 +109,25 @@ __device__ __forceinline__ float FmaSat(float a, float b, float c) {
   return d;
 }
 
+#ifdef ATMO_DEVICE_CHECKS
+// The checked build's test of a table lookup: the `bytes` at shared address
+// a lie within the block's dynamic shared memory, else the lookup reads its
+// first bytes.
+extern __shared__ float4 atmo_fast_dynamic_smem[];
+__device__ __forceinline__ uint32_t CheckedShared(uint32_t a, int bytes) {
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(atmo_fast_dynamic_smem);
+  uint32_t size;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(size));
+  return base + (uint32_t)ATMO_CHECKED_INDEX(kCheckSharedLookup, a - base,
+                                             (long long)size - bytes + 1);
+}
+#endif
+
 template <int kOffset>
 __device__ __forceinline__ float4 LoadShared4(uint32_t addr) {
+#ifdef ATMO_DEVICE_CHECKS
+  addr = CheckedShared(addr + kOffset, 16) - kOffset;
+#endif
   float4 v;
   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4+%5];"
                : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
@@ -119,6 +136,9 @@ __device__ __forceinline__ float4 LoadShared4(uint32_t addr) {
 }
 template <int kOffset>
 __device__ __forceinline__ float2 LoadShared2(uint32_t addr) {
+#ifdef ATMO_DEVICE_CHECKS
+  addr = CheckedShared(addr + kOffset, 8) - kOffset;
+#endif
   float2 v;
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(kOffset));
   return v;
@@ -428,7 +448,13 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       const int y0 = ClampIdx((int)fy, s.smu), y1 = ClampIdx((int)fy + 1, s.smu);
       const float4* src =
           (kOrder2 && sp == 1 ? in.dM : in.dR) + k * s.smu * W + n * s.smus + col;
+#ifdef ATMO_DEVICE_CHECKS
+      const long long o = src - (kOrder2 && sp == 1 ? in.dM : in.dR), nS = s.s_texels();
+      const float4 a = __ldg(src - o + ATMO_CHECKED_INDEX(kCheckDensityStage, o + y0 * W, nS));
+      const float4 b = __ldg(src - o + ATMO_CHECKED_INDEX(kCheckDensityStage, o + y1 * W, nS));
+#else
       const float4 a = __ldg(src + y0 * W), b = __ldg(src + y1 * W);
+#endif
       // At order 2 the single-scattering tables carry their phase constants.
       const float scale = kOrder2 ? (sp == 1 ? in.c.mie_k : in.c.ray_k) : 1.0f;
       v = make_float4(fmaf(wy, b.x - a.x, a.x) * scale, fmaf(wy, b.y - a.y, a.y) * scale,
@@ -734,6 +760,9 @@ __device__ __forceinline__ float UMuSFromMuSAlongRay(const Consts& c, const Shap
   return TexCoord(s, kMapSMUS, DivFtz(fmaxf(fmaf(-a, inv_A, 1.0f), 0.0f), 1.0f + a));
 }
 
+// The element at offset + x of a LUT row of a line build.
+#define ATMO_LINE_PTR(base, offset, x, n) ATMO_CHECKED_PTR(kCheckLineLoad, base, offset, x, n)
+
 // A read-only global load predicated on p: v keeps its value when p is 0.
 // The predicate keeps the line build free of branches, so a sample's loads
 // still issue as early as the unconditional ones.
@@ -751,6 +780,7 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
   const MultipleFastDims dims = MultipleDims(s);
   const int W = s.sw(), R = dims.rows, G = dims.group;
   const int rows_total = s.sr * s.smu;
+  [[maybe_unused]] const long long nS = s.s_texels();   // checked build
   const int row0 = local * R;
   RaySample* samp = reinterpret_cast<RaySample*>(smem);                 // [R][kRaySamples]
   float4* line = smem + R * kRaySamples * (int)(sizeof(RaySample) / 16);   // [2][G][R][W]
@@ -812,10 +842,10 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
         const RaySample& sm = samp[rr * kRaySamples + first + g];
         const int x = x_t;
         const int fresh = (sm.r00 != o00) | (sm.r11 != o11);
-        LoadIf(a, in.dJ + sm.r00 + x, fresh);
-        LoadIf(b, in.dJ + sm.r01 + x, fresh);
-        LoadIf(p, in.dJ + sm.r10 + x, fresh);
-        LoadIf(q, in.dJ + sm.r11 + x, fresh);
+        LoadIf(a, ATMO_LINE_PTR(in.dJ, sm.r00, x, nS), fresh);
+        LoadIf(b, ATMO_LINE_PTR(in.dJ, sm.r01, x, nS), fresh);
+        LoadIf(p, ATMO_LINE_PTR(in.dJ, sm.r10, x, nS), fresh);
+        LoadIf(q, ATMO_LINE_PTR(in.dJ, sm.r11, x, nS), fresh);
         o00 = sm.r00;
         o11 = sm.r11;
         buf[(g * R + rr) * W + x] = make_float4(
@@ -831,8 +861,10 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
         for (int m = 0; m < kCols; ++m) {
           const int x = x_t + m * kMultipleFastThreads;
           if (kCols > 1 && x >= W) break;
-          const float4 a = __ldg(in.dJ + sm.r00 + x), b = __ldg(in.dJ + sm.r01 + x);
-          const float4 p = __ldg(in.dJ + sm.r10 + x), q = __ldg(in.dJ + sm.r11 + x);
+          const float4 a = __ldg(ATMO_LINE_PTR(in.dJ, sm.r00, x, nS));
+          const float4 b = __ldg(ATMO_LINE_PTR(in.dJ, sm.r01, x, nS));
+          const float4 p = __ldg(ATMO_LINE_PTR(in.dJ, sm.r10, x, nS));
+          const float4 q = __ldg(ATMO_LINE_PTR(in.dJ, sm.r11, x, nS));
           out[x] = make_float4(
               fmaf(q.x, sm.w11, fmaf(p.x, sm.w10, fmaf(b.x, sm.w01, a.x * sm.w00))),
               fmaf(q.y, sm.w11, fmaf(p.y, sm.w10, fmaf(b.y, sm.w01, a.y * sm.w00))),
@@ -858,12 +890,14 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
           const int c2 = min(max(i0 + s.smus, 0), nmax), c3 = min(max(i0 + s.smus + 1, 0), nmax);
           const float l1 = lnu[m], l0 = 1.0f - l1;
           const float v0 = (1.0f - a) * l0, v1 = a * l0;
-          const float4 t0 = L[c0], t1 = L[c1];
+          const float4 t0 = L[ATMO_CHECKED_INDEX(kCheckLineTap, c0, W)];
+          const float4 t1 = L[ATMO_CHECKED_INDEX(kCheckLineTap, c1, W)];
           F3 S{fmaf(t1.x, v1, t0.x * v0), fmaf(t1.y, v1, t0.y * v0),
                fmaf(t1.z, v1, t0.z * v0)};
           if (l1 != 0.0f) {
             const float v2 = (1.0f - a) * l1, v3 = a * l1;
-            const float4 t2 = L[c2], t3 = L[c3];
+            const float4 t2 = L[ATMO_CHECKED_INDEX(kCheckLineTap, c2, W)];
+            const float4 t3 = L[ATMO_CHECKED_INDEX(kCheckLineTap, c3, W)];
             S = F3{fmaf(t3.x, v3, fmaf(t2.x, v2, S.x)), fmaf(t3.y, v3, fmaf(t2.y, v2, S.y)),
                    fmaf(t3.z, v3, fmaf(t2.z, v2, S.z))};
           }
@@ -878,7 +912,7 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
   for (int m = 0; m < kCols; ++m) {
     const int x = x_t + m * kMultipleFastThreads;
     if (kCols > 1 && x >= W) break;
-    const int texel = rowi * W + x;
+    const int texel = (int)ATMO_CHECKED_INDEX(kCheckOutput, rowi * W + x, nS);
     in.dR[texel] = to4(acc[m], 1.0f);   // delta multiple aliases delta Rayleigh
     const F3 add = MatVec(c.lum, acc[m]) * (1.0f / RayleighPhase(c, nu[m]));
     const float4 o = in.S[texel];
@@ -1011,6 +1045,7 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
   const MultipleFastDims dims = SingleDims(s);
   const int W = s.sw(), R = dims.rows, G = dims.group, TW = s.tw;
   const int rows_total = s.sr * s.smu;
+  [[maybe_unused]] const long long nT = s.t_texels();   // checked build
   const int row0 = local * R;
   SunSample* samp = reinterpret_cast<SunSample*>(smem);                       // [R][51]
   float4* line = smem + R * kSingleSamples * (int)(sizeof(SunSample) / 16);   // [2][G][R][TW]
@@ -1065,8 +1100,8 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
         for (int g = 0; g < count; ++g) {
           const SunSample& sm = samp[first + g];
           const int fresh = (sm.t0 != o0) | (sm.t1 != o1);
-          LoadIf(a, in.T + sm.t0 + x, fresh);
-          LoadIf(b, in.T + sm.t1 + x, fresh);
+          LoadIf(a, ATMO_LINE_PTR(in.T, sm.t0, x, nT), fresh);
+          LoadIf(b, ATMO_LINE_PTR(in.T, sm.t1, x, nT), fresh);
           o0 = sm.t0;
           o1 = sm.t1;
           buf[g * TW + x] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
@@ -1080,7 +1115,8 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
           const SunSample& sm = samp[q * kSingleSamples + first + g];
           float4* out = buf + (g * R + q) * TW;
           for (int x = threadIdx.x; x < TW; x += kMultipleFastThreads) {
-            const float4 a = __ldg(in.T + sm.t0 + x), b = __ldg(in.T + sm.t1 + x);
+            const float4 a = __ldg(ATMO_LINE_PTR(in.T, sm.t0, x, nT));
+            const float4 b = __ldg(ATMO_LINE_PTR(in.T, sm.t1, x, nT));
             out[x] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
                                  fmaf(sm.b, b.z - a.z, a.z), 0.0f);
           }
@@ -1117,7 +1153,8 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
           const float gw = Xc - f;   // weight of the lower column
           const int i_hi = TW - 1 - (int)f;
           const int i_lo = max(i_hi - 1, 0);
-          const float4 lo = L[i_lo], hi = L[max(i_hi, 0)];
+          const float4 lo = L[ATMO_CHECKED_INDEX(kCheckLineTap, i_lo, TW)];
+          const float4 hi = L[ATMO_CHECKED_INDEX(kCheckLineTap, max(i_hi, 0), TW)];
           const F3 tsun{fmaf(gw, lo.x - hi.x, hi.x), fmaf(gw, lo.y - hi.y, hi.y),
                         fmaf(gw, lo.z - hi.z, hi.z)};
           const F3 t = F3{sm.tx, sm.ty, sm.tz} * (tsun * sun);
@@ -1214,5 +1251,7 @@ cudaError_t MeasureFp32Peak(double* tflops) {
   *tflops = flops / (ms * 1e-3) / 1e12;
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
+
+ATMO_CHECK_WORD_ACCESSOR(CheckWordFast)
 
 }  // namespace atmo

@@ -86,7 +86,8 @@ __device__ F3 ScatteringNode(const float4* __restrict__ tex, const Shape& s, int
   F3 acc = f3(0.0f);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const float4 t0 = __ldg(tex + rows[q] + i0), t1 = __ldg(tex + rows[q] + i1);
+    const float4 t0 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, rows[q], i0, W * Hh * D));
+    const float4 t1 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, rows[q], i1, W * Hh * D));
     const float w0 = (1.0f - a) * wr[q], w1 = a * wr[q];
     acc.x += t0.x * w0 + t1.x * w1;
     acc.y += t0.y * w0 + t1.y * w1;
@@ -198,4 +199,17 @@ cudaError_t LaunchIndirectIrradiance(const Instance* insts, WorkList wl, int til
                                                                            smem_bytes);
   return cudaGetLastError();
 }
+
+// A check that fails by construction (index 5 of 3), with no memory access:
+// the checked build records it, the ordinary build compiles it to nothing.
+__global__ void k_check_selftest(int i, int n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) (void)ATMO_CHECKED_INDEX(kCheckSelfTest, i, n);
+}
+cudaError_t LaunchCheckSelfTest(cudaStream_t st) {
+  k_check_selftest<<<1, 32, 0, st>>>(5, 3);
+  return cudaGetLastError();
+}
+
+ATMO_CHECK_WORD_ACCESSOR(CheckWordKernels)
+
 }  // namespace atmo

@@ -49,6 +49,8 @@ cudaError_t LaunchMultipleFast(const Instance* insts, WorkList wl, int tiles, in
 // Final conversion of the scattering accumulators to half precision.
 cudaError_t LaunchToHalf(const float4* src, void* dst, long long n, cudaStream_t st);
 cudaError_t MeasureFp32Peak(double* tflops);
+// One check that fails by construction, recorded by the checked build only.
+cudaError_t LaunchCheckSelfTest(cudaStream_t st);
 
 }  // namespace atmo
 

@@ -62,4 +62,6 @@ cudaError_t LaunchMultiplePlain(const Instance* insts, WorkList wl, int tiles,
   return cudaGetLastError();
 }
 
+ATMO_CHECK_WORD_ACCESSOR(CheckWordRays)
+
 }  // namespace atmo

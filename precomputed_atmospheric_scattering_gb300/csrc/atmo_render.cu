@@ -53,7 +53,8 @@ __device__ float4 ScatteringRGBA(const float4* __restrict__ tex, const Shape& s,
     const int i0 = ClampIdx(base + (int)fx, W), i1 = ClampIdx(base + (int)fx + 1, W);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const float4 t0 = __ldg(tex + rows[q] + i0), t1 = __ldg(tex + rows[q] + i1);
+      const float4 t0 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, rows[q], i0, W * Hh * D));
+      const float4 t1 = __ldg(ATMO_CHECKED_PTR(kCheckLutTexel, tex, rows[q], i1, W * Hh * D));
       const float w0 = (1.0f - a) * wn * wr[q], w1 = a * wn * wr[q];
       acc.x += t0.x * w0 + t1.x * w1;
       acc.y += t0.y * w0 + t1.y * w1;
@@ -326,5 +327,7 @@ cudaError_t LaunchShadeView(const RenderLuts& luts, const PinholeView& v, cudaSt
       luts, v);
   return cudaGetLastError();
 }
+
+ATMO_CHECK_WORD_ACCESSOR(CheckWordRender)
 
 }  // namespace atmo

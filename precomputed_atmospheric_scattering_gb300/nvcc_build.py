@@ -12,6 +12,10 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libatmo_gb300.so")
+# The checked build (device-side index checks, csrc/atmo_check.cuh): the same
+# sources compiled with -DATMO_DEVICE_CHECKS into their own objects.
+BUILD_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(PKG, "libatmo_gb300_checked.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -43,18 +47,20 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, checked: bool = False) -> str:
+    build_dir, lib = (BUILD_CHECKED, LIB_CHECKED) if checked else (BUILD, LIB)
+    extra = ["-DATMO_DEVICE_CHECKS"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
                if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(os.path.dirname(PKG), "include", "atmo", "atmo.h"))
     objs, jobs = [], []
     for u in UNITS:
         src = os.path.join(CSRC, u)
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        obj = os.path.join(build_dir, u.replace(".cu", ".o"))
         objs.append(obj)
         if force or _stale(obj, [src] + headers + [__file__]):
-            cmd = [nvcc()] + ARCH + COMMON + UNIT_FLAGS.get(u, []) + ["-c", src, "-o", obj]
+            cmd = [nvcc()] + ARCH + COMMON + extra + UNIT_FLAGS.get(u, []) + ["-c", src, "-o", obj]
             jobs.append(cmd)
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -64,11 +70,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(r.stdout + r.stderr, file=sys.stderr)
     with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if force or jobs or _stale(lib, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         run(cmd)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, checked="--checked" in sys.argv))
