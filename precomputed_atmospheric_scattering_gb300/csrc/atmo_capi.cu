@@ -204,6 +204,7 @@ struct atmo_model {
     in.Tau = storage.Tau;
     in.I = storage.I;
     in.dI = storage.dI;
+    in.dI2 = storage.dI2;
     in.dR = storage.dR;
     in.dM = storage.dM;
     in.dJ = storage.dJ;
@@ -727,6 +728,7 @@ atmo_status atmo_batch_create(const atmo_atmosphere* atmospheres, const atmo_lut
     in.Tau = sto.Tau;
     in.I = sto.I;
     in.dI = sto.dI;
+    in.dI2 = sto.dI2;
     in.dR = sto.dR;
     in.dM = sto.dM;
     in.dJ = sto.dJ;
@@ -1237,6 +1239,7 @@ atmo_status atmo_autotune(const atmo_atmosphere* atmosphere, const atmo_lut_shap
         in.Tau = sto.Tau;
         in.I = sto.I;
         in.dI = sto.dI;
+        in.dI2 = sto.dI2;
         in.dR = sto.dR;
         in.dM = sto.dM;
         in.dJ = sto.dJ;

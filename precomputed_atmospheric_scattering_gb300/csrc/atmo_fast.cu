@@ -405,7 +405,7 @@ __device__ __forceinline__ void DensityThetaRow(DensityTask<kOrder2>& task,
 
 template <bool kOrder2>
 __global__ void __launch_bounds__(kDensityFastThreads)
-k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) {
+k_density_fast(const Instance* __restrict__ insts, WorkList wl, int order, int smem_bytes) {
   extern __shared__ float4 smem[];
   constexpr int kSpecies = kOrder2 ? 2 : 1;
   constexpr int kStride = kOrder2 ? kPairBytes : kNodeBytes;
@@ -460,7 +460,7 @@ k_density_fast(const Instance* __restrict__ insts, WorkList wl, int smem_bytes) 
       v = make_float4(fmaf(wy, b.x - a.x, a.x) * scale, fmaf(wy, b.y - a.y, a.y) * scale,
                       fmaf(wy, b.z - a.z, a.z) * scale, 0.0f);
     } else {
-      v = __ldg(in.dI + (e - kSpecies * nodes));
+      v = __ldg(DeltaIrradiance(in, order - 2) + (e - kSpecies * nodes));
     }
     V[e] = v;
   }
@@ -631,13 +631,14 @@ cudaError_t LaunchDensityFast(const Instance* insts, WorkList wl, int tiles, int
   // smem_bytes: the largest DensityFastSmem of the work list's instances.
   const size_t bytes = (size_t)smem_bytes;
   if (order == 2) {
-    k_density_fast<true><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, smem_bytes);
+    k_density_fast<true><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, order, smem_bytes);
   } else {
     if (smem_bytes > 48 * 1024) {
       const cudaError_t e = PrepareDensityFast();
       if (e != cudaSuccess) return e;
     }
-    k_density_fast<false><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, smem_bytes);
+    k_density_fast<false><<<tiles, kDensityFastThreads, bytes, st>>>(insts, wl, order,
+                                                                      smem_bytes);
   }
   return cudaGetLastError();
 }

@@ -18,6 +18,7 @@ struct Instance {
   float4* Tau;      // optical depth -ln(T) of the same texels (internal)
   float4* I;        // irradiance accumulator, W_I x H_I
   float4* dI;       // delta irradiance
+  float4* dI2;      // second delta irradiance (odd indirect orders), or nullptr: dI only
   float4* dR;       // delta Rayleigh; also delta multiple scattering (model.cc:897)
   float4* dM;       // delta Mie
   float4* dJ;       // delta scattering density
@@ -28,6 +29,13 @@ struct Instance {
   int combined;     // combine_scattering_textures
   int blend;        // accumulate into I / S / M (wavelength groups after the first)
 };
+
+// The delta irradiance of indirect order k (0: the direct pass).  With two
+// buffers the indirect pass of order k + 1 writes the other one while the
+// density pass of order k + 2 reads this one, so the two can run at once.
+ATMO_HD float4* DeltaIrradiance(const Instance& in, int k) {
+  return (k & 1) && in.dI2 ? in.dI2 : in.dI;
+}
 
 // A launch covers `count` instances; instance inst[q] owns the tiles
 // [start[q], start[q+1]).  Both arrays live in device memory.

@@ -173,7 +173,7 @@ k_indirect_irradiance(const Instance* __restrict__ insts, WorkList wl, int order
     acc.z += __shfl_xor_sync(0xffffffffu, acc.z, off);
   }
   if (valid && lane == 0) {
-    in.dI[texel] = to4(acc, 1.0f);
+    DeltaIrradiance(in, order)[texel] = to4(acc, 1.0f);
     F3 add = MatVec(in.c.lum, acc);
     float4 o = in.I[texel];
     in.I[texel] = make_float4(o.x + add.x, o.y + add.y, o.z + add.z, o.w);

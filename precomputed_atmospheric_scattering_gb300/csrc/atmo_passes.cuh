@@ -289,7 +289,8 @@ ATMO_PASS F3 ScatteringDensityTexel(const Instance& in, long long texel, int ord
         // Ground point: |(0, 0, r) + omega_i * dist| = Rb, so the normal's
         // cosine with the sun is (r mu_s + dist nu1) / Rb.
         float mu_g = fmaf(dr.dist_ground, nu1, row.r * ang.mu_s) / c.Rb;
-        radiance = fma3(tg, Irradiance(c, s, in.dI, 0.0f, mu_g), radiance);
+        radiance = fma3(tg, Irradiance(c, s, DeltaIrradiance(in, order - 2), 0.0f, mu_g),
+                        radiance);
       }
       float nu2 = fmaf(ang.omega_x, ox, ang.mu * dr.cos_t);
       row_sum = fma3(radiance, a_r * RayleighPhase(c, nu2) + a_m * MiePhase(c, nu2), row_sum);

@@ -93,6 +93,7 @@ atmo_status Storage::Allocate(const Shape& shape, bool combined_textures, bool h
   ATMO_ALLOC(Tau, nT * sizeof(float4));
   ATMO_ALLOC(I, nI * sizeof(float4));
   ATMO_ALLOC(dI, nI * sizeof(float4));
+  ATMO_ALLOC(dI2, nI * sizeof(float4));
   ATMO_ALLOC(dR, nS * sizeof(float4));
   ATMO_ALLOC(dM, nS * sizeof(float4));
   ATMO_ALLOC(dJ, nS * sizeof(float4));
@@ -115,7 +116,7 @@ atmo_status Storage::Allocate(const Shape& shape, bool combined_textures, bool h
 void Storage::Free() {
   for (void* p : owned) cudaFree(p);
   owned.clear();
-  T = Tau = I = dI = dR = dM = dJ = S = M = nullptr;
+  T = Tau = I = dI = dI2 = dR = dM = dJ = S = M = nullptr;
   S_half = M_half = nullptr;
   tab = Tables{};
 }
@@ -123,7 +124,7 @@ void Storage::Free() {
 size_t Storage::Bytes() const {
   const size_t nT = (size_t)s.t_texels(), nI = (size_t)s.i_texels(),
                nS = (size_t)s.s_texels();
-  size_t b = (2 * nT + 2 * nI) * 16 + nS * 16 * (4 + (combined ? 0 : 1));
+  size_t b = (2 * nT + 3 * nI) * 16 + nS * 16 * (4 + (combined ? 0 : 1));
   if (half) b += nS * 8 * (combined ? 1 : 2);
   b += (size_t)s.sr * s.smu * sizeof(TexelRow) + s.smus * sizeof(TexelCol) +
        (size_t)s.sr * kDensityThetaSamples * sizeof(DensityRow) + s.ih * sizeof(IrrRow) +
@@ -214,6 +215,9 @@ int Tiles(Pass pass, const Shape& s, atmo_path path) {
 Program::~Program() {
   if (graph_) cudaGraphExecDestroy(graph_);
   if (capture_stream_) cudaStreamDestroy(capture_stream_);
+  if (side_stream_) cudaStreamDestroy(side_stream_);
+  if (ev_fork_) cudaEventDestroy(ev_fork_);
+  if (ev_join_) cudaEventDestroy(ev_join_);
   if (upload_done_) cudaEventDestroy(upload_done_);
   if (d_slots_) cudaFree(d_slots_);
   if (h_slots_pinned_) cudaFreeHost(h_slots_pinned_);
@@ -308,6 +312,9 @@ atmo_status Program::Finalize() {
   // Row orders of the instances that have the table (slots of one model share
   // it; the radii of a later set_atmosphere leave the order stale, which
   // changes nothing in the LUTs).
+  fork_indirect_ = !slots.empty();
+  for (const Instance& in : slots)
+    if (!in.dI2 || in.dI2 == in.dI) fork_indirect_ = false;
   std::vector<int*> done;
   for (const Instance& in : slots) {
     if (!in.tab.row_order ||
@@ -338,6 +345,28 @@ atmo_status Program::Upload(cudaStream_t st) {
 
 atmo_status Program::Launch(cudaStream_t st) {
   for (size_t i = 0; i < steps_.size(); ++i) {
+    // The indirect irradiance of order n - 1 runs beside the density pass of
+    // order n: they write and read different delta-irradiance buffers and
+    // both only read the previous order's scattering, which the multiple
+    // scattering of order n overwrites after joining both.  The indirect
+    // pass's small grid then fills the density launch's gaps.
+    if (fork_indirect_ && steps_[i].pass == Pass::kDensity && i + 1 < steps_.size() &&
+        steps_[i + 1].pass == Pass::kIndirect && steps_[i + 1].order == steps_[i].order - 1) {
+      if (!side_stream_) {
+        ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking));
+        ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+        ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+      }
+      ATMO_CUDA_TRY(cudaEventRecord(ev_fork_, st));
+      ATMO_CUDA_TRY(cudaStreamWaitEvent(side_stream_, ev_fork_, 0));
+      atmo_status s = LaunchStep(i + 1, side_stream_);
+      if (s != ATMO_OK) return s;
+      ATMO_CUDA_TRY(cudaEventRecord(ev_join_, side_stream_));
+      if ((s = LaunchStep(i, st)) != ATMO_OK) return s;
+      ATMO_CUDA_TRY(cudaStreamWaitEvent(st, ev_join_, 0));
+      ++i;
+      continue;
+    }
     atmo_status s = LaunchStep(i, st);
     if (s != ATMO_OK) return s;
   }

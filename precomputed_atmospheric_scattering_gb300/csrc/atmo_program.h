@@ -34,8 +34,8 @@ struct Storage {
   Shape s{};
   bool combined = true;
   bool half = false;
-  float4 *T = nullptr, *Tau = nullptr, *I = nullptr, *dI = nullptr, *dR = nullptr, *dM = nullptr,
-         *dJ = nullptr, *S = nullptr, *M = nullptr;
+  float4 *T = nullptr, *Tau = nullptr, *I = nullptr, *dI = nullptr, *dI2 = nullptr,
+         *dR = nullptr, *dM = nullptr, *dJ = nullptr, *S = nullptr, *M = nullptr;
   void *S_half = nullptr, *M_half = nullptr;   // half-precision outputs
   Tables tab{};
   std::vector<void*> owned;                    // what Free() releases
@@ -95,6 +95,11 @@ class Program {
   cudaStream_t capture_stream_ = nullptr;
   cudaEvent_t upload_done_ = nullptr;    // guards reuse of the pinned staging copy
   bool finalized_ = false;
+  // Indirect irradiance beside density (every slot has two delta-irradiance
+  // buffers): the side stream and the fork / join events of Launch.
+  bool fork_indirect_ = false;
+  cudaStream_t side_stream_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
 };
 
 // The kernel variant that runs `pass` for shape s when `path` is requested:
