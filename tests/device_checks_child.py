@@ -4,9 +4,10 @@ run_workloads(atmo) runs, through the package's public API, rebuilds that
 reach every kernel and index path of the precomputation -- a combined batch of
 uneven shapes (the minimal and an odd shape, NU 16 with a wide irradiance LUT,
 the half, default and double-R shapes, 2 to 5 orders), a separate-texture
-batch, the plain kernels, the high-resolution shape (4 line columns per
-thread, rows in the order of their rays' invariant) and the render queries and
-a shading request -- and returns their outputs as host arrays.
+batch, the plain kernels, the 15-wavelength FP16 model, the server's rounds
+and shading, the high-resolution shape (4 line columns per thread, rows in the
+order of their rays' invariant) and the render queries and a shading request
+-- and returns their outputs as host arrays.
 
 Run as a script with ATMO_LIBRARY=checked, it loads the checked build of the
 library, runs the workloads, reads the check record, then launches the
@@ -87,6 +88,34 @@ def run_workloads(atmo):
     atmo.precompute(W.earth(), PLAIN_SHAPE, 4, T, S, None, I, path=atmo.PATH_PLAIN)
     torch.cuda.synchronize()
     out["pT"], out["pS"], out["pI"] = T.cpu().numpy(), S.cpu().numpy(), I.cpu().numpy()
+
+    # The 15-wavelength FP16 model (5 wavelength groups blending into the same
+    # LUTs, the luminance matrices, the transmittance recomputed, FP16 output).
+    m = W.spectral_earth_model(PLAIN_SHAPE)
+    m.Init(4)
+    out["mT"], out["mS"] = m.transmittance(), m.scattering()
+    out["mM"], out["mI"] = m.single_mie_scattering(), m.irradiance()
+    del m
+
+    # The server: pool-carved instances, rebuilds of two shapes built in
+    # rounds beside each other, then a shading request on one of them.
+    srv = atmo.Server()
+    ids = [srv.submit_rebuild(W.earth(), PLAIN_SHAPE, 3),
+           srv.submit_rebuild(W.earth(mie_g=0.7), (128, 32, 8, 32, 16, 8, 32, 8), 4)]
+    for t in ids:
+        srv.wait(t)
+    view = W.random_view(rng, 6360.0, width=96, height=54)
+    depth = torch.from_numpy(rng.uniform(0.1, 100.0, 96 * 54).astype(np.float32)).to(dev)
+    sky_t = torch.empty((54, 96, 4), device=dev)
+    shaded_t = torch.empty_like(sky_t)
+    srv.wait(srv.submit_shade(ids[1], view, depth, sky_t, shaded_t))
+    for j, t in enumerate(ids):
+        lut = srv.lut_set(t)
+        for k, kind in kinds.items():
+            out["v%d%s" % (j, k)] = lut.read(kind)
+        del lut
+    out["v_sky"], out["v_shaded"] = sky_t.cpu().numpy(), shaded_t.cpu().numpy()
+    srv.close()
 
     b = atmo.Batch([W.hires_earth()], [HIRES], 3)
     b.run()

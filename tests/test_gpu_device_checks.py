@@ -6,8 +6,9 @@ memory table lookups, line-build rows and taps, staged texels, the texels of
 every LUT lookup), records the first failure and reads element 0 instead.
 A child process loads that build (ATMO_LIBRARY=checked) and runs rebuilds
 over the minimal, odd, NU-16, half, default, double-R and high-resolution
-shapes on the fast and plain kernels, both texture layouts, and the render
-queries and a shading request: no check may fail, and the results must equal
+shapes on the fast and plain kernels, both texture layouts, the 15-wavelength
+FP16 model, the server's rounds and shading, and the render queries and a
+shading request: no check may fail, and the results must equal
 the ordinary build's (the checks change no arithmetic, but the compiler
 schedules the checked code differently, hence a tolerance of a few ulps).
 The self-test check, which fails by construction without touching memory,
@@ -56,7 +57,10 @@ def test_checked_build_matches_the_ordinary_build(checked_run, atmo):
         assert got.shape == want.shape, k
         scale = np.maximum(np.abs(want), 1e-6 * np.abs(want).max() + 1e-30)
         err = float(np.max(np.abs(got - want) / scale))
-        assert err <= 1e-5, "%s differs from the ordinary build by %g" % (k, err)
+        # The FP16 model's LUTs ("m*"): one FP16 ulp if an FP32 value rounds
+        # the other way.
+        tol = 2.0 ** -10 if k.startswith("m") else 1e-5
+        assert err <= tol, "%s differs from the ordinary build by %g" % (k, err)
 
 
 def test_ordinary_build_has_no_checks(atmo):
