@@ -277,9 +277,11 @@ k_query(const RenderLuts q, const QueryArrays x, int kind) {
 
 // One pixel of a shading request: the three queries of the reference's API
 // along the pixel's view ray.
-// 8 blocks per SM (64 registers, a few spills) beat 6 at 80 registers by 6%:
-// the kernel waits on its LUT gathers.
-__global__ void __launch_bounds__(kQueryThreads, 8)
+// 6 blocks per SM (80 registers, 76 bytes of spills) beat 8 at 64 registers
+// (276 bytes of spills) by 3% and 7 at 72 registers by 1-3%, with the
+// approximate division and square root of this file (with IEEE division, 8
+// blocks had been 6% faster than 6).
+__global__ void __launch_bounds__(kQueryThreads, 6)
 k_shade_view(const RenderLuts q, const PinholeView v) {
   const long long pix = (long long)blockIdx.x * kQueryThreads + threadIdx.x;
   if (pix >= (long long)v.width * v.height) return;
