@@ -343,6 +343,14 @@ atmo_status Program::Upload(cudaStream_t st) {
   return ATMO_OK;
 }
 
+atmo_status Program::PrepareFork() {
+  if (!fork_indirect_ || side_stream_) return ATMO_OK;
+  ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking));
+  ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+  ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+  return ATMO_OK;
+}
+
 atmo_status Program::Launch(cudaStream_t st) {
   for (size_t i = 0; i < steps_.size(); ++i) {
     // The indirect irradiance of order n - 1 runs beside the density pass of
@@ -352,15 +360,11 @@ atmo_status Program::Launch(cudaStream_t st) {
     // pass's small grid then fills the density launch's gaps.
     if (fork_indirect_ && steps_[i].pass == Pass::kDensity && i + 1 < steps_.size() &&
         steps_[i + 1].pass == Pass::kIndirect && steps_[i + 1].order == steps_[i].order - 1) {
-      if (!side_stream_) {
-        ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking));
-        ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
-        ATMO_CUDA_TRY(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
-      }
+      atmo_status s = PrepareFork();
+      if (s != ATMO_OK) return s;
       ATMO_CUDA_TRY(cudaEventRecord(ev_fork_, st));
       ATMO_CUDA_TRY(cudaStreamWaitEvent(side_stream_, ev_fork_, 0));
-      atmo_status s = LaunchStep(i + 1, side_stream_);
-      if (s != ATMO_OK) return s;
+      if ((s = LaunchStep(i + 1, side_stream_)) != ATMO_OK) return s;
       ATMO_CUDA_TRY(cudaEventRecord(ev_join_, side_stream_));
       if ((s = LaunchStep(i, st)) != ATMO_OK) return s;
       ATMO_CUDA_TRY(cudaStreamWaitEvent(st, ev_join_, 0));
@@ -468,8 +472,10 @@ atmo_status Program::Run(cudaStream_t st, bool use_graph) {
       ATMO_CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
     }
     cudaGraph_t g = nullptr;
-    // Kernel attributes are set before the capture, not inside it.
+    // Kernel attributes, the side stream and its events are set up before
+    // the capture, not inside it.
     ATMO_CUDA_TRY(PrepareDensityFast());
+    if ((s = PrepareFork()) != ATMO_OK) return s;
     ATMO_CUDA_TRY(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
     atmo_status ls = Launch(capture_stream_);
     cudaError_t ce = cudaStreamEndCapture(capture_stream_, &g);

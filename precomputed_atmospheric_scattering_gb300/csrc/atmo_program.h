@@ -98,6 +98,7 @@ class Program {
   // Indirect irradiance beside density (every slot has two delta-irradiance
   // buffers): the side stream and the fork / join events of Launch.
   bool fork_indirect_ = false;
+  atmo_status PrepareFork();             // creates the side stream and events once
   cudaStream_t side_stream_ = nullptr;
   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
 };
