@@ -19,14 +19,14 @@ names a directory, to bench_detail.json there.  Reported:
                  come back device->host into pinned memory inside the timed
                  region (two batches alternate, so a step's read-back overlaps
                  the next step's rebuilds),
-  the benchmark spec     single-rebuild p50 latency (fast path), the plain per-texel
-                 kernels' rebuilds/s and the batched / plain ratio,
+  single_and_plain  single-rebuild p50 / p99 latency (fast path), the plain
+                 per-texel kernels' rebuilds/s and the batched / plain ratio,
   roofline       the scattering-density kernel (the dominant one) against this
                  GPU's FP32 FMA throughput measured in the same run: the FP32
                  operations the kernel executes per direction sample (ncu SASS
                  op counters) x samples / launch time; the reference
                  algorithm's operation count (tests/golden/flops_config0.json)
-                 over the same time is reported apart, as algorithmic_rate,
+                 over the same time is reported apart, as algorithmic_tflops,
   parity         per-LUT max / p99 relative error of the benchmarked LUTs at
                  the FP64 reference's committed sampled texels,
   configs        the spectral-precision (15 wavelengths, FP16 LUTs) and the
@@ -424,7 +424,7 @@ def run_gpu(args):
     clk = clocks.summary()
     if rank != 0:
         return
-    north = {"single_p50_ms": p50, "single_p99_ms": p99,
+    single_plain = {"single_p50_ms": p50, "single_p99_ms": p99,
              "plain_rebuilds_per_s": 1000.0 / plain_ms,
              "batched_vs_plain": value / (1000.0 / plain_ms) / world}
     cpu = cpu_baseline_entry() if not args.no_cpu_baseline else None
@@ -433,7 +433,7 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: the reference demo's Earth",
-        "north_star": north,
+        "single_and_plain": single_plain,
         "config": {"workload": WORKLOAD, "batch": B, "orders": 4,
                    "parallelism": "replicas (independent batches "
                    "per GPU)" if world > 1 else "single GPU",
@@ -457,7 +457,7 @@ def run_gpu(args):
             "shade": [serving["shade_ms"]["p50"], serving["shade_ms"]["p99"]]}
     detail = {"config": {"lut_shape": list(shape), "tuning": tuning,
                          "warm_up": {"steps": warm_steps, "seconds": round(warm_s, 2)}},
-              "north_star": north, "launch_gaps": launch_gaps, "roofline": roof,
+              "single_and_plain": single_plain, "launch_gaps": launch_gaps, "roofline": roof,
               "passes_ms": passes_ms,
               "parity": parity, "configs": configs, "batched_mixed": mixed,
               "serving": serving, "serving_half_rate": half_rate, "cpu_baseline": cpu}
