@@ -9,7 +9,7 @@
  *   atmosphere/reference/model.cc:73-245 (CPU pass driver)
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
- * this library, and only as the checker or the timed CPU baseline.  The
+ * this library, and only to check results or as the timed CPU baseline.  The
  * product (libatmo_gb300.so) never links or calls it.
  *
  * Textures cross this interface as double RGBA arrays, x fastest, then y,

@@ -595,7 +595,7 @@ atmo_status atmo_model_set_program_uniforms(const atmo_model* m, unsigned, unsig
                                             unsigned, unsigned) {
   if (!m) return Fail(ATMO_INVALID_ARG, "NULL model");
   return Fail(ATMO_UNAVAILABLE,
-              "OpenGL texture binding is unavailable: this build has no graphics stack; use "
+              "OpenGL texture binding is unavailable: this library has no graphics stack; use "
               "atmo_model_get_lut device buffers");
 }
 
