@@ -1101,16 +1101,20 @@ __device__ __forceinline__ void SingleFastBlock(const Instance& in, int local, f
       // a branch per case, or with selects, measured slower.
       const int x = threadIdx.x;
       if (x < TW && row0 < rows_total) {
+        // The thread's columns addressed once, as in multiple scattering.
         int o0 = -1, o1 = -1;
         float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+        const float4* col = in.T + x;
+        float4* out_col = buf + x;
+        const SunSample* srow = samp + first;
         for (int g = 0; g < count; ++g) {
-          const SunSample& sm = samp[first + g];
+          const SunSample& sm = srow[g];
           const int fresh = (sm.t0 != o0) | (sm.t1 != o1);
-          LoadIf(a, ATMO_LINE_PTR(in.T, sm.t0, x, nT), fresh);
-          LoadIf(b, ATMO_LINE_PTR(in.T, sm.t1, x, nT), fresh);
+          LoadIf(a, ATMO_LINE_PTR(col, sm.t0, 0, nT - x), fresh);
+          LoadIf(b, ATMO_LINE_PTR(col, sm.t1, 0, nT - x), fresh);
           o0 = sm.t0;
           o1 = sm.t1;
-          buf[g * TW + x] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
+          out_col[g * TW] = make_float4(fmaf(sm.b, b.x - a.x, a.x), fmaf(sm.b, b.y - a.y, a.y),
                                         fmaf(sm.b, b.z - a.z, a.z), 0.0f);
         }
       }
