@@ -880,9 +880,11 @@ __device__ __forceinline__ void MultipleFastBlock(const Instance& in, int local,
     }
     __syncthreads();
     if (active) {
+      const RaySample* srow = samp + rr * kRaySamples + first;
+      const float4* lrow = buf + rr * W;
       for (int g = 0; g < count; ++g) {
-        const RaySample& sm = samp[rr * kRaySamples + first + g];
-        const float4* L = buf + (g * R + rr) * W;
+        const RaySample& sm = srow[g];
+        const float4* L = lrow + g * R * W;
 #pragma unroll
         for (int m = 0; m < kCols; ++m) {
           if (kCols > 1 && x_t + m * kMultipleFastThreads >= W) break;
