@@ -122,3 +122,26 @@ def test_batch_copy_lut_is_stream_ordered(atmo, oracle, torch):
     np.testing.assert_array_equal(pin.numpy(), ref)
     with pytest.raises(atmo.AtmoError):
         b.copy_lut(0, atmo.LUT_SCATTERING, dev.data_ptr(), v.bytes - 16, copy_stream)
+
+
+def test_forked_graph_matches_sequential_passes(atmo, oracle, torch):
+    """A batch's CUDA graph runs the indirect irradiance of order n - 1 on a
+    branch beside the density pass of order n (two delta-irradiance buffers);
+    time_passes launches the same passes one after another.  Every replay of
+    the graph must give the sequential run's LUTs bit for bit (a race between
+    the branches would show as a difference on some replay)."""
+    rng = np.random.default_rng(8)
+    default = (256, 64, 32, 128, 32, 8, 64, 16)
+    atms = [oracle.earth_atmosphere()] + [random_atmosphere(oracle, rng) for _ in range(3)]
+    shapes = [default, default, SHAPES[1], SHAPES[0]]
+    b = atmo.Batch(atms, shapes, [4, 5, 3, 6])
+    kinds = (atmo.LUT_TRANSMITTANCE, atmo.LUT_SCATTERING, atmo.LUT_IRRADIANCE)
+    b.time_passes()
+    atmo.synchronize_stream()
+    want = [[b.read(i, k) for k in kinds] for i in range(len(atms))]
+    for _ in range(6):
+        b.run()
+        atmo.synchronize_stream()
+        for i in range(len(atms)):
+            for k, w in zip(kinds, want[i]):
+                np.testing.assert_array_equal(b.read(i, k), w)
